@@ -1,0 +1,360 @@
+#!/usr/bin/env python3
+"""Benchmark: SZx blocked codec on GB300, compress + decompress GB/s.
+
+Workload (default ``c2``): 512^3 float32 Gaussian random field with a k^-5/3
+spectrum (seeded FFT synthesis, unit variance) plus 5% zero-valued z-slabs,
+REL bound 1e-3, fastMode 3 (random-access layout), blockSize 128.
+
+A step is one compress and one decompress of the whole field.
+  value      = 2 * field bytes / (compress time + decompress time)   [GB/s]
+               device-resident input/output, SZxG_compress / SZxG_decompress,
+               CUDA events on the launching stream
+  e2e        = the same metric through the reference-facing C entry points
+               SZx_fast_compress_args / SZx_fast_decompress with host buffers
+               (pinned input; malloc'd outputs as the reference API returns),
+               host<->device copies inside the timed region (wall clock: the
+               calls are synchronous)
+  roofline   = the dominant kernel's algorithmic bytes per launch / its mean
+               launch time (CUDA events the library records around each launch)
+               against the measured HBM copy bandwidth
+  cpu_baseline / --impl reference = the oracle's block-parallel (OpenMP) port of
+               the reference codec on the host cores
+
+Multi-GPU: replicas only (one independent field per rank), value summed.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+REL = 1
+WORKLOADS = {
+    "c2": dict(shape=(512, 512, 512), mode=3, bs=128, rel=1e-3,
+               desc="512^3 float32 k^-5/3 Gaussian random field + 5% zero slabs, REL 1e-3, fastMode 3, blockSize 128"),
+    "c2m1": dict(shape=(512, 512, 512), mode=1, bs=128, rel=1e-3,
+                 desc="512^3 float32 k^-5/3 Gaussian random field + 5% zero slabs, REL 1e-3, fastMode 1"),
+}
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def read_traffic(kernel: str):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == kernel and parts[1] == "bytes_per_element":
+                return float(parts[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.rows = []
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 3 + k and r[3 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_field(wl, seed, device):
+    import torch
+
+    from szx_gb300 import synth
+    return synth.spectral_field(wl["shape"], seed=seed, device=device, dtype=torch.float32)
+
+
+def cpu_codec_gbs(x_np, eb, bs, reps, threads):
+    """The oracle's OpenMP port of the reference mode-3 codec: GB/s of
+    2*bytes/(t_compress + t_decompress), best of `reps`."""
+    import numpy as np
+
+    import oracle as O
+    if not os.path.exists(O.ORACLE_SO):
+        O.build(reference=False)
+    buf = np.empty(O.capacity(3, 0, x_np.size, bs), np.uint8)
+    out = np.empty_like(x_np)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        _, n = O.compress_m3_omp(x_np, eb, bs, threads=threads, out=buf)
+        t1 = time.perf_counter()
+        O.decompress_m3_omp(np.float32, buf, n, x_np.size, threads=threads, out=out)
+        t2 = time.perf_counter()
+        t = t2 - t0
+        best = t if best is None or t < best else best
+    return 2 * x_np.nbytes / best / 1e9, best
+
+
+def run_reference(args, wl, rank, world):
+    import numpy as np
+    import torch
+    if rank != 0:
+        return
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    x = make_field(wl, 1234, dev).cpu().numpy()
+    import oracle as O
+    r = O.value_range(x)[0]
+    eb = float(np.float32(np.float32(r) * np.float32(wl["rel"])))
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_codec_gbs(x, eb, wl["bs"], 1, threads)
+    times = []
+    for _ in range(args.steps):
+        _, t = cpu_codec_gbs(x, eb, wl["bs"], 1, threads)
+        times.append(t)
+    ms = 1000 * sum(times) / len(times)
+    val = 2 * x.nbytes / (sum(times) / len(times)) / 1e9
+    sample = f"whole field ({x.size} float32 values, {x.nbytes >> 20} MiB), compress+decompress per step"
+    line = {
+        "metric": "compress/decompress GB/s (fp32 REL 1e-3)", "value": round(val, 3), "unit": "GB/s",
+        "impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded on-device FFT synthesis)", "config": {"workload": wl["desc"], "elements": x.size},
+        "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import szx_gb300 as S
+    from szx_gb300._lib import lib, libc
+
+    dist = world > 1
+    if dist:
+        import torch.distributed as D
+    torch.cuda.set_device(local_rank)
+    L = lib()
+    x = make_field(wl, 1234 + rank, "cuda")
+    n = x.numel()
+    in_bytes = n * 4
+    mode, bs, rel = wl["mode"], wl["bs"], wl["rel"]
+    codec = S.DeviceCodec(mode, np.float32, n, bs)
+    y = torch.empty_like(x)
+
+    # one step to learn where the stream lands (same input every step)
+    codec.compress(x, REL, 0.0, rel)
+    info = codec.stream_info()
+    assert info.status == 0, S.SZxError(info.status, "compress")
+    off, size = int(info.offset), int(info.size)
+    sv = codec.out[off:off + size]
+
+    def step(ev=None, k=0):
+        if ev:
+            ev[3 * k].record()
+        codec.compress(x, REL, 0.0, rel)
+        if ev:
+            ev[3 * k + 1].record()
+        codec.decompress(sv, n, out=y)
+        if ev:
+            ev[3 * k + 2].record()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        D.barrier()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local_rank) if rank == 0 else None
+    time.sleep(0.3)
+    L.SZxG_trace_enable(1)
+    torch.cuda.synchronize()
+    t_start.record()
+    for k in range(args.steps):
+        step(ev, k)
+    t_end.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    names = C.create_string_buffer(4096)
+    tms = (C.c_double * 32)()
+    cnt = (C.c_ulonglong * 32)()
+    nk = L.SZxG_trace_collect(names, 4096, tms, cnt, 32)
+    L.SZxG_trace_enable(0)
+    kern = {nm: (tms[i], int(cnt[i])) for i, nm in enumerate(names.value.decode().split("\n")[:nk])}
+    total_ms = t_start.elapsed_time(t_end)
+    tc = sum(ev[3 * k].elapsed_time(ev[3 * k + 1]) for k in range(args.steps))
+    td = sum(ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(args.steps))
+    launches = sum(c for _, c in kern.values())
+    info2 = codec.stream_info()
+    assert (int(info2.offset), int(info2.size), info2.status) == (off, size, 0)
+
+    # the decoded field honours the bound (size-independent property)
+    eb = float(info.eb)
+    err = (x.double() - y.double()).abs()
+    ulp = torch.nextafter(x.abs(), torch.full_like(x, float("inf"))) - x.abs()
+    bound_ok = bool((err <= eb + 2 * ulp.double()).all().item())
+
+    if dist:
+        t = torch.tensor([total_ms, tc, td, launches], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        D.all_reduce(tmax[:3], op=D.ReduceOp.MAX)
+        D.all_reduce(t[3:], op=D.ReduceOp.SUM)
+        total_ms, tc, td = tmax[0].item(), tmax[1].item(), tmax[2].item()
+        launches = int(t[3].item())
+
+    # ---- e2e through the reference-facing entry points, host buffers
+    xh = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    xh.copy_(x.cpu())
+    free = libc().free
+    sz = C.c_size_t()
+
+    def e2e_step():
+        p = L.SZx_fast_compress_args(mode, 0, C.c_void_p(xh.data_ptr()), C.byref(sz), REL, 0.0, rel, 0.0, 0.0,
+                                     0, 0, 0, 0, n)
+        if not p:
+            raise S.SZxError(S.api.last_error(), "SZx_fast_compress_args")
+        q = L.SZx_fast_decompress(mode, 0, C.c_void_p(p), sz.value, 0, 0, 0, 0, n)
+        if not q:
+            raise S.SZxError(S.api.last_error(), "SZx_fast_decompress")
+        free(p)
+        free(q)
+        return sz.value
+
+    for _ in range(args.warmup):
+        e2e_step()
+    if dist:
+        D.barrier()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if dist:
+        tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        D.all_reduce(tt, op=D.ReduceOp.MAX)
+        e2e_s = tt.item()
+
+    if rank != 0:
+        return
+    K = args.steps
+    value = world * 2 * in_bytes * K / ((tc + td) / 1000) / 1e9
+    peak, peak_kind = read_peaks()
+    # dominant kernel and its roofline
+    enc = "blocked_encode" if mode != 1 else "nonblocked_encode"
+    dec = "blocked_decode" if mode != 1 else "nonblocked_decode"
+    dom = max((enc, dec), key=lambda k: kern.get(k, (0, 0))[0])
+    dms, dcnt = kern[dom]
+    alg = in_bytes + size          # encode: read field, write stream; decode: read stream, write field
+    achieved = alg / (dms / dcnt / 1000) / 1e9
+    tb = read_traffic(dom)
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                "traffic": round(tb * n) if tb else None, "algorithmic_bytes": alg}
+    # CPU baseline: the same field on the host cores
+    x_np = x.cpu().numpy()
+    threads = os.cpu_count() or 1
+    cpu_val, _ = cpu_codec_gbs(x_np, eb, bs, 2, threads)
+    line = {
+        "metric": "compress/decompress GB/s (fp32 REL 1e-3)",
+        "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded on-device FFT synthesis; no dataset ships with the reference)",
+        "config": {"workload": wl["desc"], "elements": n, "stream_bytes": size, "ratio": round(in_bytes / size, 4),
+                   "bound": eb, "l2": "inputs (512 MiB) larger than L2; no flush needed",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "compress_gbs": round(world * in_bytes * K / (tc / 1000) / 1e9, 2),
+        "decompress_gbs": round(world * in_bytes * K / (td / 1000) / 1e9, 2),
+        "kernels_ms_per_step": {k: round(v[0] / K, 4) for k, v in kern.items()},
+        "gpu_launches": launches,
+        "bound_ok": bound_ok,
+        "clocks": clk,
+        "e2e": {"value": round(world * 2 * in_bytes / e2e_s / 1e9, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": in_bytes + size, "d2h_bytes_per_step": size + in_bytes,
+                "api": "SZx_fast_compress_args + SZx_fast_decompress (host buffers)"},
+        "roofline": roofline,
+        "cpu_baseline": {"value": round(cpu_val, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"the same field ({n} float32 values), compress+decompress, best of 2"},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as D
+        torch.cuda.set_device(local_rank)
+        D.init_process_group("nccl")
+    run_ours(args, wl, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as D
+        D.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

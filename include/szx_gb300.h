@@ -1,0 +1,172 @@
+/*
+ * szx_gb300 -- SZx's blocked error-bounded codec on one NVIDIA GB300 (sm_103a).
+ *
+ * Part 1 is a drop-in for the reference's C API (szcompressor/SZx,
+ * szx/include/szx.h): same symbol names, argument meaning, stream format and
+ * ownership rules.  Outputs are malloc'd host buffers the caller free()s;
+ * failures return NULL (or 0) and leave a code readable with
+ * SZxG_get_last_error().  All compute runs on the current CUDA device; there
+ * is no CPU fallback.
+ *
+ * Part 2 (SZxG_*) is this library's own device-pointer interface: explicit
+ * block size, caller-provided device buffers and workspace, a CUDA stream,
+ * and no host synchronisation on the compress path.
+ *
+ * Plain pointers and sizes only; a CUDA stream is passed as void*.
+ */
+#ifndef SZX_GB300_H
+#define SZX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Constants of the reference, szx/include/szx_defines.h:19-21,36-37,54-57. */
+#define SZx_FLOAT 0
+#define SZx_DOUBLE 1
+#define ABS 0
+#define REL 1
+#define FXR 2
+#define SZx_NO_BLOCK_FAST_CMPR 1
+#define SZx_WITH_BLOCK_FAST_CMPR 2
+#define SZx_RANDOMACCESS_FAST_CMPR 3
+#define SZx_OPENMP_FAST_CMPR 4
+
+/* =====================================================================
+ * Part 1: reference C API (szx/include/szx.h:28-102)
+ * ===================================================================== */
+
+/* szx/include/szx.h:72, szx/src/szx.cc:41-71 */
+int SZx_computeDimension(size_t r5, size_t r4, size_t r3, size_t r2, size_t r1);
+/* szx/include/szx.h:73, szx/src/szx.cc:73-101 */
+size_t SZx_computeDataLength(size_t r5, size_t r4, size_t r3, size_t r2, size_t r1);
+/* szx/include/szx.h:74, szx/src/szx.cc:109-229 */
+int SZx_filterDimension(size_t r5, size_t r4, size_t r3, size_t r2, size_t r1, size_t* correctedDimension);
+
+/* szx/include/szx.h:75-76, szx/src/szx.cc:231-348.  Block size 128 as in the
+ * reference.  fastMode 1, 2, 3, 4; ABS / REL / FXR.  Returns a malloc'd stream. */
+unsigned char* SZx_fast_compress_args(int fastMode, int dataType, void* data, size_t* outSize, int errBoundMode,
+                                      float absErrBound, float relBoundRatio, float compressionRatio, float tolerance,
+                                      size_t r5, size_t r4, size_t r3, size_t r2, size_t r1);
+
+/* szx/include/szx.h:78, szx/src/szx.cc:378-430.  fastMode 1, 3, 4.  Returns a
+ * malloc'd array of SZx_computeDataLength(r5..r1) values. */
+void* SZx_fast_decompress(int fastMode, int dataType, unsigned char* bytes, size_t byteLength, size_t r5, size_t r4,
+                          size_t r3, size_t r2, size_t r1);
+
+/* szx/include/szx.h:79, szx/src/szx.cc:432-438 */
+double SZx_computeValueRange(void* oriData, int dataType, size_t length, float* radius, float* medianValue);
+
+/* szx/include/szx.h:80-82, szx/src/szx.cc:441-448: mode-4 layout (native-endian
+ * constant medians) with an explicit block size. */
+unsigned char* SZx_fast_compress_args_unpredictable_blocked_randomaccess_openmp(void* oriData, int dataType,
+                                                                                size_t* outSize, float absErrBound,
+                                                                                size_t nbEle, int blockSize);
+/* szx/include/szx.h:83, szx/src/szx.cc:450-456 */
+void* SZx_fast_decompress_args_unpredictable_blocked_randomaccess_openmp(int dataType, size_t nbEle,
+                                                                         unsigned char* cmpBytes);
+
+/* szx/include/szx.h:85, szx/src/szx.cc:458-464.  Fixed-rate bound search of
+ * the reference (sampled-block ratio estimator + bracketing + bisection). */
+float SZx_estimateErrorBoundbasedonCR(int dataType, float targetCompressionRatio, float tolerance, void* data,
+                                      float initErrorBound, int blockSize, size_t nbEle);
+
+/* szx/include/szx.h:87, szx/src/szx.cc:466-473: mode-2 layout, explicit block size. */
+unsigned char* SZx_fast_compress_args_unpredictable_blocked(void* oriData, int dataType, size_t* outSize,
+                                                            float absErrBound, size_t nbEle, int blockSize);
+
+/* szx/include/szx.h:89, szx/src/szx.cc:475-485: copies every samplingRate-th
+ * block into *buffer and returns the sampled value range. */
+float computeRadiusBuffer(void* oriData, int dataType, size_t nbEle, int samplingRate, int blockSize,
+                          float** radiusArray, float** mediusArray, void* buffer);
+
+/* szx/include/szx.h:91-92, szx/src/szx.cc:487-498 */
+float estimateCRbasedonErrorBound_buffered(int dataType, float errorBound, void* buffer, float* medianArray,
+                                          float* radiusArray, int samplingRate, int blockSize, size_t nbEle,
+                                          size_t* sumReqNbBytes, size_t* sum_actual_leadNumbers);
+
+/* szx/include/szx.h:95, szx/src/szx.cc:501-512: mode-2 stream into a caller
+ * buffer; returns its size (0 for double data, as the reference does). */
+size_t SZx_fast_compress_args_unpredictable_blocked_args(void* oriData, int dataType, unsigned char* outputBytes,
+                                                         float absErrBound, size_t nbEle, int blockSize);
+
+/* szx/include/szx.h:96, szx/src/szx.cc:514-524: *(float**)newData receives a
+ * malloc'd array (float data only, as in the reference). */
+void SZx_fast_decompress_args_unpredictable_blocked(void* newData, int dataType, size_t nbEle,
+                                                   unsigned char* cmpBytes);
+
+/* =====================================================================
+ * Part 2: device-pointer interface (no counterpart in the reference)
+ * ===================================================================== */
+
+/* Error codes. */
+#define SZXG_OK 0
+#define SZXG_ERR_LOOKBACK 1   /* a device-wide scan gave up waiting (bounded spin) */
+#define SZXG_ERR_CAPACITY 2   /* output buffer too small */
+#define SZXG_ERR_STREAM 3     /* malformed or truncated stream */
+#define SZXG_ERR_ARG 4        /* invalid argument */
+#define SZXG_ERR_CUDA 5       /* CUDA runtime error */
+#define SZXG_ERR_UNSUPPORTED 6
+
+int SZxG_get_last_error(void);
+const char* SZxG_error_string(int code);
+
+/* Where a compressed stream sits in a device output buffer. */
+typedef struct {
+    unsigned long long offset;   /* stream start, relative to the output buffer */
+    unsigned long long size;     /* stream length in bytes */
+    unsigned long long nb_const; /* constant blocks (blocked layouts) */
+    float eb;                    /* absolute bound used */
+    int status;                  /* SZXG_* code */
+} SZxG_StreamInfo;
+
+/* Worst-case output bytes for one compress call (stream + alignment slack). */
+size_t SZxG_compress_bound(int fastMode, int dataType, size_t nbEle, int blockSize);
+/* Device scratch bytes one compress or decompress call needs. */
+size_t SZxG_workspace_size(int fastMode, int dataType, size_t nbEle, int blockSize);
+
+/* Enqueue a compress of nbEle device values on `stream`.  The stream lands at
+ * d_out + info.offset; *d_info (device memory) receives the info.  Nothing is
+ * synchronised.  blockSize 1..256 (2..255 for fastMode 2). */
+int SZxG_compress(int fastMode, int dataType, const void* d_data, size_t nbEle, int blockSize, int errBoundMode,
+                  float absErrBound, float relBoundRatio, void* d_out, size_t outCapacity, void* d_workspace,
+                  size_t workspaceBytes, SZxG_StreamInfo* d_info, void* stream);
+
+/* Enqueue a decompress of a device-resident stream into nbEle device values.
+ * blockSize must be the stream's (blocked layouts); 0 reads it from the
+ * stream with a synchronous 20-byte copy. */
+int SZxG_decompress(int fastMode, int dataType, const void* d_stream, size_t streamBytes, size_t nbEle,
+                    int blockSize, void* d_out, void* d_workspace, size_t workspaceBytes, void* stream);
+
+/* Read back the status a previous SZxG_* call left in its workspace (waits
+ * for `stream`). */
+int SZxG_workspace_status(const void* d_workspace, void* stream);
+
+/* Host-buffer codec with an explicit block size (same stream as Part 1). */
+unsigned char* SZxG_compress_host(int fastMode, int dataType, const void* data, size_t nbEle, int blockSize,
+                                  int errBoundMode, float absErrBound, float relBoundRatio, size_t* outSize);
+void* SZxG_decompress_host(int fastMode, int dataType, const unsigned char* bytes, size_t byteLength, size_t nbEle);
+
+/* Host-buffer codec into caller-provided host memory (pinned memory gives
+ * full-speed copies).  Returns the stream size, 0 on failure. */
+size_t SZxG_compress_host_into(int fastMode, int dataType, const void* data, size_t nbEle, int blockSize,
+                               int errBoundMode, float absErrBound, float relBoundRatio, unsigned char* out,
+                               size_t outCapacity);
+int SZxG_decompress_host_into(int fastMode, int dataType, const unsigned char* bytes, size_t byteLength, size_t nbEle,
+                              void* out);
+
+/* Launch tracing: CUDA events around every kernel this library enqueues.
+ * enable(1) starts (and clears) a trace, enable(0) stops and clears it.
+ * collect() waits for the recorded events and writes, per kernel name, the
+ * summed milliseconds and launch count; names are '\n'-separated in `names`.
+ * Returns the number of kernels reported. */
+void SZxG_trace_enable(int on);
+int SZxG_trace_collect(char* names, size_t names_len, double* ms, unsigned long long* counts, int max_kernels);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SZX_GB300_H */

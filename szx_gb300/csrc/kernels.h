@@ -1,0 +1,123 @@
+// Host-visible launchers and device-resident structures of the SZx codec.
+// Shared by the kernels (*.cu) and the C-ABI layer (api.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace szxg {
+
+// Parameters derived on the device from the data (value range pass) so that a
+// relative bound never needs a host round trip.
+struct CodecParams {
+    float eb;          // absolute bound the codec uses (ABS passthrough or range * ratio)
+    float radius;      // global radius (non-blocked layout), szx/src/szx_float.cc:494
+    float median;      // global median (non-blocked layout), szx/src/szx_float.cc:495
+    float range_f;     // value range as float (float data)
+    double range_d;    // value range as double (double data)
+    int has_range;
+    int pad;
+};
+
+// Totals written by the last tile of an encode and read by the assembler.
+struct Totals {
+    unsigned long long payload_bytes;  // bytes of non-constant payloads / mid bytes
+    unsigned long long nnc;            // non-constant blocks
+};
+
+// Where the finished stream sits inside the caller's output buffer.
+struct StreamResult {
+    unsigned long long offset;   // stream start relative to the output buffer
+    unsigned long long size;     // stream length in bytes
+    unsigned long long nb_const; // constant blocks (blocked layouts)
+    float eb;                    // bound used
+    int status;                  // 0 ok, otherwise an SZxG error code
+};
+
+// Header of a blocked stream parsed on the device (decode).
+struct BlockedHdr {
+    unsigned long long bs, nb, nc, nnc, sb;
+    unsigned long long o_off, s_off, m_off, q_off;  // byte offsets in the stream
+    unsigned long long n;
+    int ok;
+    int pad;
+};
+
+// Header of a non-blocked stream parsed on the device (decode).
+struct NonBlockedHdr {
+    unsigned long long n, L, mid_off, mid_len;
+    float median;
+    int reqLength;
+    int ok;
+};
+
+enum Layout : int { kNonBlocked = 1, kBlocked = 2, kRandomAccess = 3, kRandomAccessNative = 4 };
+
+// ------------------------------------------------------------------ workspace
+
+// Device scratch needed by one compress or decompress call; carved by
+// ws_carve() out of one caller-provided allocation.
+struct Workspace {
+    CodecParams* params;
+    Totals* totals;
+    StreamResult* result;
+    BlockedHdr* bhdr;
+    NonBlockedHdr* nhdr;
+    int* err;
+    unsigned long long* counters;   // 4 tile counters
+    unsigned long long* st_word;    // tile status words (family A)
+    unsigned long long* st_agg2;
+    unsigned long long* st_inc2;
+    unsigned long long* st2_word;   // tile status (family B)
+    unsigned long long* st2_agg2;
+    unsigned long long* st2_inc2;
+    void* partials;                 // range-pass partials
+    uint16_t* o_scr;                // payload sizes by non-constant rank
+    uint32_t* m_scr;                // median bits by constant rank
+    uint8_t* s_scr;                 // state bits
+    unsigned long long* p_off;      // decode: payload offsets by non-constant rank
+    uint32_t* rank_w;               // decode: non-constant rank at each 32-block word
+    unsigned long long* tile_aux;   // non-blocked decode: per-tile summaries
+    size_t status_tiles, status2_tiles, blocks, words, aux_tiles;
+};
+
+size_t ws_bytes(int layout, int dtype, size_t n, int bs);
+Workspace ws_carve(void* base, int layout, int dtype, size_t n, int bs);
+
+// ------------------------------------------------------------------ launchers (return cudaError_t)
+
+// Global value range + derived bound; writes *params.  err_mode 0 = ABS, 1 = REL.
+cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float abs_eb, float rel,
+                         const Workspace& ws, cudaStream_t s);
+
+// Blocked encode (layouts 2, 3, 4): stats + encode + placement + header assembly.
+// d_out must hold blocked_bound() bytes; the stream lands at d_out + result.offset.
+size_t blocked_bound(int layout, int dtype, size_t n, int bs);
+cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
+                                  float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s);
+// Blocked decode (layouts 3, 4).
+cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream, size_t len, size_t n, int bs,
+                                  void* d_out, const Workspace& ws, cudaStream_t s);
+
+// Non-blocked (layout 1) encode / decode.
+size_t nonblocked_bound(int dtype, size_t n);
+cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t* d_out, size_t cap,
+                                     const Workspace& ws, cudaStream_t s);
+cudaError_t launch_nonblocked_decode(int dtype, const uint8_t* d_stream, size_t len, size_t n, void* d_out,
+                                     const Workspace& ws, cudaStream_t s);
+
+int sm_count();
+
+// Records CUDA events around one kernel launch when tracing is enabled
+// (SZxG_trace_enable); a no-op otherwise.
+class TraceScope {
+  public:
+    TraceScope(const char* name, cudaStream_t s);
+    ~TraceScope();
+  private:
+    const char* name_;
+    cudaStream_t s_;
+    void* a_;
+};
+
+}  // namespace szxg

@@ -1,0 +1,560 @@
+// Non-blocked layout of the SZx stream (fastMode 1):
+//   SZx_fast_compress_args_unpredictable_float, szx/src/szx_float.cc:1492-1699
+//   (double: szx/src/szx_double.cc:1593-2011), decoded by
+//   szx/src/szxd_float.cc:478-662 (double: szx/src/szxd_double.cc:683-1114).
+//
+//   [1,1,1,0] | reqLength u8 | median f32 BE | leadBytes u64 BE | 2-bit lead
+//   codes for all N values | mid bytes
+//
+// One global median/radius (from the value-range pass) and ONE XOR chain over
+// the whole array: each value's lead code depends only on its predecessor, so
+// codes are data-parallel; mid-byte positions need a device-wide prefix sum
+// (decoupled look-back over 4096-value tiles).  Decoding must also find, for
+// every value, the last earlier value that stored each of the top three byte
+// lanes -- possibly many tiles back -- which a per-tile look-back of
+// "latest writer tile" indices (packed max) resolves in the same pass that
+// places the tiles' mid bytes.
+//
+// The stream is placed 15 bytes into the output buffer so the lead-code array
+// (stream offset 17) starts 16-byte aligned.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace szxg {
+
+constexpr int kNbThreads = 256;
+constexpr int kNbPer = 16;                        // values per thread
+constexpr int kNbTile = kNbThreads * kNbPer;      // 4096 values per tile
+constexpr unsigned long long kNbShift = 15;
+
+// CTA-wide exclusive sum (256 threads), returns the total through *tot.
+__device__ __forceinline__ uint32_t cta_excl_sum32(uint32_t v, uint32_t* tot, uint32_t* sm /*[8]*/) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t incl = warp_inclusive_sum(v);
+    if (lane == 31) sm[warp] = incl;
+    __syncthreads();
+    uint32_t pre = 0, t = 0;
+#pragma unroll
+    for (int w = 0; w < kNbThreads / 32; w++) {
+        uint32_t x = sm[w];
+        pre += w < warp ? x : 0;
+        t += x;
+    }
+    __syncthreads();
+    *tot = t;
+    return pre + incl - v;
+}
+
+// Copy [sh, sh+n) of a 16-aligned shared buffer to global dst (dst % 16 == sh).
+__device__ __forceinline__ void cta_copy_out(const uint8_t* stage, uint32_t sh, uint32_t n, uint8_t* dst) {
+    uint8_t* gbase = dst - sh;
+    const uint32_t end = sh + n, nch = (end + 15) >> 4;
+    for (uint32_t c = threadIdx.x; c < nch; c += blockDim.x) {
+        uint32_t lo = c << 4, hi = lo + 16;
+        if (lo >= sh && hi <= end) *(uint4*)(gbase + lo) = *(const uint4*)(stage + lo);
+        else {
+            uint32_t a = lo > sh ? lo : sh, b = hi < end ? hi : end;
+            for (uint32_t j = a; j < b; j++) gbase[j] = stage[j];
+        }
+    }
+}
+
+// Stage [src, src+n) into a 16-aligned shared buffer at offset src % 16; bytes
+// outside [s0, s1) are never read.
+__device__ __forceinline__ void cta_copy_in(uint8_t* stage, const uint8_t* src, uint32_t n, const uint8_t* s0,
+                                            const uint8_t* s1) {
+    const uint32_t sh = (uint32_t)((uintptr_t)src & 15);
+    const uint8_t* gbase = src - sh;
+    const uint32_t nch = (sh + n + 15) >> 4;
+    for (uint32_t c = threadIdx.x; c < nch; c += blockDim.x) {
+        const uint8_t* lo = gbase + (c << 4);
+        if (lo >= s0 && lo + 16 <= s1) *(uint4*)(stage + (c << 4)) = __ldg((const uint4*)lo);
+        else
+            for (int j = 0; j < 16; j++) stage[(c << 4) + j] = (lo + j >= s0 && lo + j < s1) ? lo[j] : 0;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void load16(const T* p, unsigned long long first, unsigned long long n, T (&v)[kNbPer]) {
+    const bool full = first + kNbPer <= n;
+    if (full && ((uintptr_t)(p + first) % 16) == 0) {
+        const uint4* q = (const uint4*)(p + first);
+#pragma unroll
+        for (int i = 0; i < kNbPer * (int)sizeof(T) / 16; i++) {
+            uint4 w = q[i];
+            if constexpr (sizeof(T) == 4) {
+                v[4 * i] = __uint_as_float(w.x); v[4 * i + 1] = __uint_as_float(w.y);
+                v[4 * i + 2] = __uint_as_float(w.z); v[4 * i + 3] = __uint_as_float(w.w);
+            } else {
+                v[2 * i] = __longlong_as_double((long long)(((unsigned long long)w.y << 32) | w.x));
+                v[2 * i + 1] = __longlong_as_double((long long)(((unsigned long long)w.w << 32) | w.z));
+            }
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < kNbPer; e++) v[e] = first + e < n ? p[first + e] : (T)0;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void store16(T* p, unsigned long long first, unsigned long long n, const T (&v)[kNbPer]) {
+    const bool full = first + kNbPer <= n;
+    if (full && ((uintptr_t)(p + first) % 16) == 0) {
+        uint4* q = (uint4*)(p + first);
+#pragma unroll
+        for (int i = 0; i < kNbPer * (int)sizeof(T) / 16; i++) {
+            uint4 w;
+            if constexpr (sizeof(T) == 4) {
+                w = make_uint4(__float_as_uint(v[4 * i]), __float_as_uint(v[4 * i + 1]), __float_as_uint(v[4 * i + 2]),
+                               __float_as_uint(v[4 * i + 3]));
+            } else {
+                unsigned long long a = (unsigned long long)__double_as_longlong(v[2 * i]);
+                unsigned long long b = (unsigned long long)__double_as_longlong(v[2 * i + 1]);
+                w = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32));
+            }
+            q[i] = w;
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < kNbPer; e++)
+            if (first + e < n) p[first + e] = v[e];
+    }
+}
+
+// ------------------------------------------------------------------ encode
+
+struct NbEncArgs {
+    const void* x;
+    unsigned long long n, ntiles, cap;
+    const CodecParams* params;
+    uint8_t* out;
+    TileStatus st;
+    unsigned long long* tile_ctr;
+    int* err;
+    StreamResult* res;
+};
+
+__device__ __forceinline__ void or_bytes_nb(uint32_t* buf, uint32_t q, unsigned long long ev, int cnt) {
+    if (cnt <= 0) return;
+    uint32_t sh = (q & 3) * 8;
+    uint32_t* w = buf + (q >> 2);
+    unsigned long long lo = ev << sh;
+    atomicOr(w, (uint32_t)lo);
+    int span = (int)(q & 3) + cnt;
+    if (span > 4) atomicOr(w + 1, (uint32_t)(lo >> 32));
+    if (span > 8) atomicOr(w + 2, (uint32_t)(ev >> (64 - sh)));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
+    using EL = Elem<T>;
+    using U = typename EL::U;
+    constexpr int W = EL::W;
+    __shared__ __align__(16) uint8_t stage[kNbTile * W + 48];
+    __shared__ uint32_t s_sum[8];
+    __shared__ long long s_tile;
+    __shared__ unsigned long long s_base;
+    __shared__ int s_skip;
+    const T* x = (const T*)a.x;
+    const CodecParams P = *a.params;
+    // szx/src/szx_float.cc:1514-1535 / szx_double.cc:1615-1636
+    bool zm;
+    const int reqLength = req_length<T>(P.eb, P.radius, &zm);
+    int R, s;
+    split_reqlen(reqLength, &R, &s);
+    T med;
+    if constexpr (sizeof(T) == 4) med = zm ? 0.0f : P.median;
+    else med = (double)P.median;
+    const uint32_t med_stored = zm ? 0u : __float_as_uint(P.median);
+    const unsigned long long L = (a.n + 3) / 4;
+    uint8_t* lead = a.out + kNbShift + 17;
+    uint8_t* mid = lead + L;
+    const unsigned long long mid_cap = a.cap - (kNbShift + 17 + L);
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(a.tile_ctr, 1ull);
+        __syncthreads();
+        const long long tile = s_tile;
+        if (tile >= (long long)a.ntiles) break;
+        const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
+        T v[kNbPer];
+        load16<T>(x, first, a.n, v);
+        U cur[kNbPer];
+#pragma unroll
+        for (int e = 0; e < kNbPer; e++) cur[e] = EL::bits(EL::sub(v[e], med)) >> s;
+        U prev = __shfl_up_sync(0xffffffffu, cur[kNbPer - 1], 1);
+        if (lane == 0) prev = first > 0 && first - 1 < a.n ? (EL::bits(EL::sub(x[first - 1], med)) >> s) : (U)0;
+        uint32_t codes = 0, mine = 0;
+#pragma unroll
+        for (int e = 0; e < kNbPer; e++) {
+            U xr = cur[e] ^ (e ? cur[e - 1] : prev);
+            int lz;
+            if constexpr (sizeof(T) == 4) lz = __clz(xr) >> 3;
+            else lz = __clzll((long long)xr) >> 3;
+            int ld = lz < 3 ? lz : 3;
+            if (first + e < a.n) {
+                codes |= (uint32_t)ld << (8 * (e >> 2) + 6 - 2 * (e & 3));
+                int c = R - ld;
+                mine += c > 0 ? c : 0;
+            }
+        }
+        uint32_t total;
+        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);
+        if (threadIdx.x < 32) {
+            unsigned long long base, dummy;
+            lookback(a.st, tile, total, 0, &base, &dummy, a.err);
+            if (threadIdx.x == 0) {
+                s_base = base;
+                const bool ok = base + total <= mid_cap;
+                s_skip = !ok;
+                if (!ok) atomicExch(a.err, kErrCapacity);
+                if (tile == (long long)a.ntiles - 1) {
+                    uint8_t* h = a.out + kNbShift;
+                    h[0] = 1; h[1] = 1; h[2] = 1; h[3] = 0;
+                    h[4] = (uint8_t)reqLength;
+                    h[5] = (uint8_t)(med_stored >> 24); h[6] = (uint8_t)(med_stored >> 16);
+                    h[7] = (uint8_t)(med_stored >> 8); h[8] = (uint8_t)med_stored;
+                    for (int k = 0; k < 8; k++) h[9 + k] = (uint8_t)(L >> (56 - 8 * k));
+                    StreamResult r;
+                    r.offset = kNbShift;
+                    r.size = 17 + L + base + total;
+                    r.nb_const = 0;
+                    r.eb = P.eb;
+                    r.status = 0;
+                    *a.res = r;
+                }
+            }
+        }
+        __syncthreads();   // s_base / s_skip from the look-back
+        // lead codes: 4 bytes per thread
+        const unsigned long long lb = first >> 2;
+        if (lb + 4 <= L && ((uintptr_t)(lead + lb) & 3) == 0) *(uint32_t*)(lead + lb) = codes;
+        else
+            for (int j = 0; j < 4; j++)
+                if (lb + j < L) lead[lb + j] = (uint8_t)(codes >> (8 * j));
+        // mid bytes via shared staging
+        const unsigned long long base = s_base;
+        const uint32_t sh = (uint32_t)((uintptr_t)(mid + base) & 15);
+        const uint32_t nz = (sh + total + 16 + 15) >> 4;
+        for (uint32_t i = threadIdx.x; i < nz; i += kNbThreads) ((uint4*)stage)[i] = make_uint4(0, 0, 0, 0);
+        __syncthreads();
+        if (!s_skip) {
+            uint32_t q = sh + ex;
+            uint32_t* buf = (uint32_t*)stage;
+#pragma unroll
+            for (int e = 0; e < kNbPer; e++) {
+                int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+                int c = R - ld;
+                if (first + e < a.n && c > 0) {
+                    unsigned long long ev = (unsigned long long)(cur[e] >> (8 * (W - R)));
+                    ev &= c >= 8 ? ~0ull : ((1ull << (8 * c)) - 1);
+                    or_bytes_nb(buf, q, ev, c);
+                    q += c;
+                }
+            }
+        }
+        __syncthreads();
+        if (!s_skip) cta_copy_out(stage, sh, total, mid + base);
+        __syncthreads();
+    }
+}
+
+size_t nonblocked_bound(int dtype, size_t n) {
+    size_t es = dtype == 0 ? 4 : 8;
+    return kNbShift + 17 + (n + 3) / 4 + es * n + 64;
+}
+
+cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t* d_out, size_t cap,
+                                     const Workspace& ws, cudaStream_t s) {
+    if (n == 0 || cap < nonblocked_bound(dtype, n) - 64) return cudaErrorInvalidValue;
+    const size_t ntiles = (n + kNbTile - 1) / kNbTile;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(ws.st_word, 0, sizeof(unsigned long long) * ntiles, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ws.counters, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ws.err, 0, sizeof(int), s)) != cudaSuccess) return e;
+    NbEncArgs a;
+    a.x = x; a.n = n; a.ntiles = ntiles; a.cap = cap; a.params = ws.params; a.out = d_out;
+    a.st = TileStatus{ws.st_word, ws.st_agg2, ws.st_inc2};
+    a.tile_ctr = &ws.counters[0];
+    a.err = ws.err;
+    a.res = ws.result;
+    size_t g = (size_t)sm_count() * (dtype == 0 ? 6 : 4);
+    int grid = (int)(ntiles < g ? ntiles : g);
+    {
+        TraceScope tr("nonblocked_encode", s);
+        if (dtype == 0) k_nb_encode<float><<<grid, kNbThreads, 0, s>>>(a);
+        else k_nb_encode<double><<<grid, kNbThreads, 0, s>>>(a);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // fold the error word into the result
+    return cudaSuccess;
+}
+
+// ------------------------------------------------------------------ decode
+
+__global__ void k_nb_parse(const uint8_t* s, unsigned long long len, unsigned long long n, NonBlockedHdr* h,
+                           int* err) {
+    NonBlockedHdr r = {};
+    r.n = n;
+    r.ok = 0;
+    if (len >= 17 && s[3] == 0) {
+        unsigned long long L = 0;
+        for (int k = 0; k < 8; k++) L = (L << 8) | s[9 + k];
+        r.L = L;
+        r.reqLength = s[4];
+        r.median = __uint_as_float(((uint32_t)s[5] << 24) | ((uint32_t)s[6] << 16) | ((uint32_t)s[7] << 8) | s[8]);
+        r.mid_off = 17 + L;
+        r.ok = L == (n + 3) / 4 && r.mid_off <= len && r.reqLength >= 1 && r.reqLength <= 64;
+        r.mid_len = r.ok ? len - r.mid_off : 0;
+    }
+    *h = r;
+    *err = r.ok ? kErrNone : kErrStream;
+}
+
+__device__ __forceinline__ uint32_t lead_word(const uint8_t* lead, unsigned long long lb, unsigned long long L) {
+    uint32_t w = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) w |= (lb + j < L ? (uint32_t)lead[lb + j] : 0u) << (8 * j);
+    return w;
+}
+
+// Per-tile mid-byte count and, for the top three byte lanes, where in the
+// tile's mid bytes the last value storing that lane put it.  Look-back over
+// tiles yields each tile's mid-byte offset and the latest earlier tile that
+// stored each lane.  aux[3t] = offset, aux[3t+1] = latest writer tiles (3x21
+// bits, tile+1), aux[3t+2] = own writer positions (3x21 bits, pos+1).
+template <typename T>
+__global__ void __launch_bounds__(kNbThreads) k_nb_summary(const uint8_t* s, const NonBlockedHdr* hp,
+                                                           unsigned long long* aux, TileStatus st,
+                                                           unsigned long long* ctr, int* err) {
+    constexpr int W = Elem<T>::W;
+    __shared__ uint32_t s_sum[8];
+    __shared__ int s_pos[3][8];
+    __shared__ long long s_tile;
+    const NonBlockedHdr h = *hp;
+    if (!h.ok) return;
+    int R, sft;
+    split_reqlen(h.reqLength, &R, &sft);
+    if (R > W) return;
+    const unsigned long long ntiles = (h.n + kNbTile - 1) / kNbTile;
+    const uint8_t* lead = s + 17;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(ctr, 1ull);
+        __syncthreads();
+        const long long tile = s_tile;
+        if (tile >= (long long)ntiles) break;
+        const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
+        const uint32_t codes = lead_word(lead, first >> 2, h.L);
+        uint32_t mine = 0;
+        int lpos[3] = {-1, -1, -1};
+        for (int e = 0; e < kNbPer; e++) {
+            if (first + e >= h.n) break;
+            int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+            int c = R - ld;
+            if (c > 0) {
+#pragma unroll
+                for (int k = 0; k < 3; k++)   // lane W-1-k is stored when ld <= k (and is required when k <= R-1)
+                    if (ld <= k && k <= R - 1) lpos[k] = (int)mine + (R - 1 - k);
+                mine += c;
+            }
+        }
+        uint32_t total;
+        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);
+        int gpos[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            int p = lpos[k] >= 0 ? (int)ex + lpos[k] : -1;
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) p = max(p, __shfl_xor_sync(0xffffffffu, p, d));
+            if (lane == 0) s_pos[k][warp] = p;
+        }
+        __syncthreads();
+        unsigned long long own = 0, latest = 0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            int p = -1;
+            for (int w = 0; w < kNbThreads / 32; w++) p = max(p, s_pos[k][w]);
+            gpos[k] = p;
+            own |= (unsigned long long)(p + 1) << (21 * k);
+            if (p >= 0) latest |= (unsigned long long)(tile + 1) << (21 * k);
+        }
+        if (threadIdx.x < 32) {
+            unsigned long long base, lw;
+            lookback<Max3x21Op>(st, tile, total, latest, &base, &lw, err);
+            if (threadIdx.x == 0) {
+                aux[3 * tile] = base;
+                aux[3 * tile + 1] = lw;
+                aux[3 * tile + 2] = own;
+                if (tile == (long long)ntiles - 1 && base + total > h.mid_len) atomicExch(err, kErrStream);
+            }
+        }
+        (void)gpos;
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kNbThreads) k_nb_decode(const uint8_t* __restrict__ s, unsigned long long len,
+                                                          const NonBlockedHdr* hp,
+                                                          const unsigned long long* __restrict__ aux, T* out,
+                                                          unsigned long long* ctr) {
+    using EL = Elem<T>;
+    using U = typename EL::U;
+    constexpr int W = EL::W;
+    constexpr int TOPSH = 8 * (W - 3);
+    __shared__ __align__(16) uint8_t stage[kNbTile * W + 48];
+    __shared__ uint32_t s_sum[8];
+    __shared__ uint32_t s_wsum[8];
+    __shared__ long long s_tile;
+    const NonBlockedHdr h = *hp;
+    if (!h.ok) return;
+    int R, sft;
+    split_reqlen(h.reqLength, &R, &sft);
+    if (R > W) return;
+    const unsigned long long ntiles = (h.n + kNbTile - 1) / kNbTile;
+    const uint8_t* lead = s + 17;
+    const uint8_t* mid = s + h.mid_off;
+    const uint8_t* send = s + len;
+    const T med = (T)h.median;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(ctr, 1ull);
+        __syncthreads();
+        const long long tile = s_tile;
+        if (tile >= (long long)ntiles) break;
+        const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
+        const uint32_t codes = lead_word(lead, first >> 2, h.L);
+        int cnt[kNbPer];
+        uint32_t mine = 0;
+#pragma unroll
+        for (int e = 0; e < kNbPer; e++) {
+            int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+            int c = R - ld;
+            cnt[e] = (first + e < h.n && c > 0) ? c : 0;
+            mine += cnt[e];
+        }
+        uint32_t total;
+        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);
+        const unsigned long long tbase = aux[3 * tile];
+        // carried bytes at the tile start: the latest earlier tile that stored each lane
+        uint32_t carry = 0;
+        {
+            const unsigned long long lw = aux[3 * tile + 1];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                unsigned long long t1 = (lw >> (21 * k)) & 0x1FFFFF;
+                if (t1) {
+                    unsigned long long u = t1 - 1;
+                    unsigned long long p1 = (aux[3 * u + 2] >> (21 * k)) & 0x1FFFFF;
+                    unsigned long long pos = h.mid_off + aux[3 * u] + (p1 - 1);
+                    uint32_t byte = pos < len ? s[pos] : 0u;
+                    carry |= byte << (8 * (2 - k));   // lane W-1-k sits at bits 8*(2-k) of the packed top bytes
+                }
+            }
+        }
+        // stage this tile's mid bytes
+        const uint8_t* src = mid + tbase;
+        cta_copy_in(stage, src, total, s, send);
+        __syncthreads();
+        const uint32_t sh = (uint32_t)((uintptr_t)src & 15);
+        const uint32_t* buf = (const uint32_t*)stage;
+        uint32_t q = sh + ex;
+        U sp[kNbPer];
+#pragma unroll
+        for (int e = 0; e < kNbPer; e++) {
+            uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
+            uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
+            if constexpr (sizeof(T) == 4) {
+                uint32_t m = cnt[e] >= 4 ? 0xFFFFFFFFu : ((1u << (8 * cnt[e])) - 1);
+                sp[e] = (lo & m) << (8 * (W - R));
+            } else {
+                uint32_t w2 = buf[(q >> 2) + 2];
+                uint32_t hi = __funnelshift_r(w1, w2, (q & 3) * 8);
+                unsigned long long v = ((unsigned long long)hi << 32) | lo;
+                unsigned long long m = cnt[e] >= 8 ? ~0ull : ((1ull << (8 * cnt[e])) - 1);
+                sp[e] = (v & m) << (8 * (W - R));
+            }
+            q += cnt[e];
+        }
+        // packed last-writer summary of the top three byte lanes (see blocked.cu)
+        uint32_t sv = 0, sm = 0;
+#pragma unroll
+        for (int e = 0; e < kNbPer; e++) {
+            if (first + e < h.n) {
+                int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+                uint32_t wm = (1u << (3 - ld)) - 1;
+                uint32_t wb = (wm & 1) * 0xFFu | (wm & 2) * 0x7F80u | (wm & 4) * 0x3FC000u;
+                uint32_t top = (uint32_t)(sp[e] >> TOPSH) & 0xFFFFFFu;
+                sv = (sv & ~wb) | (top & wb);
+                sm |= wm;
+            }
+        }
+        auto comb = [](uint32_t A, uint32_t B) {
+            uint32_t bm = B >> 24;
+            uint32_t wb = (bm & 1) * 0xFFu | (bm & 2) * 0x7F80u | (bm & 4) * 0x3FC000u;
+            return (((A >> 24) | bm) << 24) | ((A & 0xFFFFFFu & ~wb) | (B & 0xFFFFFFu & wb));
+        };
+        uint32_t sum = (sm << 24) | sv;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t o = __shfl_up_sync(0xffffffffu, sum, d);
+            if (lane >= d) sum = comb(o, sum);
+        }
+        if (lane == 31) s_wsum[warp] = sum;
+        __syncthreads();
+        uint32_t wpre = (7u << 24) | carry;
+        for (int w = 0; w < warp; w++) wpre = comb(wpre, s_wsum[w]);
+        uint32_t exs = __shfl_up_sync(0xffffffffu, sum, 1);
+        uint32_t full = lane ? comb(wpre, exs) : wpre;
+        U prev = (U)(full & 0xFFFFFFu) << TOPSH;
+        T v[kNbPer];
+#pragma unroll
+        for (int e = 0; e < kNbPer; e++) {
+            int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+            U inh = ld ? ~(((U)1 << (8 * (W - ld))) - 1) : (U)0;
+            U cur = sp[e] | (prev & inh);
+            v[e] = EL::add(EL::of(cur << sft), med);
+            prev = cur;
+        }
+        store16<T>(out, first, h.n, v);
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_nonblocked_decode(int dtype, const uint8_t* d_stream, size_t len, size_t n, void* d_out,
+                                     const Workspace& ws, cudaStream_t s) {
+    if (n == 0) return cudaErrorInvalidValue;
+    const size_t ntiles = (n + kNbTile - 1) / kNbTile;
+    if (ntiles >= (1u << 21) - 1) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(ws.st_word, 0, sizeof(unsigned long long) * ntiles, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ws.counters, 0, 2 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
+    {
+        TraceScope tr("nonblocked_parse", s);
+        k_nb_parse<<<1, 1, 0, s>>>(d_stream, len, n, ws.nhdr, ws.err);
+    }
+    size_t g = (size_t)sm_count() * 8;
+    int grid = (int)(ntiles < g ? ntiles : g);
+    TileStatus st{ws.st_word, ws.st_agg2, ws.st_inc2};
+    {
+        TraceScope tr("nonblocked_summary", s);
+        if (dtype == 0)
+            k_nb_summary<float><<<grid, kNbThreads, 0, s>>>(d_stream, ws.nhdr, ws.tile_aux, st, &ws.counters[0], ws.err);
+        else
+            k_nb_summary<double><<<grid, kNbThreads, 0, s>>>(d_stream, ws.nhdr, ws.tile_aux, st, &ws.counters[0],
+                                                             ws.err);
+    }
+    {
+        TraceScope tr("nonblocked_decode", s);
+        if (dtype == 0)
+            k_nb_decode<float><<<grid, kNbThreads, 0, s>>>(d_stream, len, ws.nhdr, ws.tile_aux, (float*)d_out,
+                                                           &ws.counters[1]);
+        else
+            k_nb_decode<double><<<grid, kNbThreads, 0, s>>>(d_stream, len, ws.nhdr, ws.tile_aux, (double*)d_out,
+                                                            &ws.counters[1]);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace szxg
