@@ -30,6 +30,42 @@ static inline double f64_of(uint64_t u) { double v; memcpy(&v, &u, 8); return v;
  * in the codec is a LOGICAL shift of the unsigned pattern
  * (szx/src/szx_float.cc:92, szx/src/szx_double.cc:76, szx/src/szxd_float.cc:117-119). */
 
+/* IEEE arithmetic with the NaN results of x86-64 SSE, the reference's native
+ * platform: a NaN operand is returned quieted (the first operand when both
+ * are NaN), an invalid operation (inf - inf, 0/0, ...) returns the negative
+ * "indefinite" quiet NaN, and float<->double conversions carry the payload.
+ * Written out explicitly so that the oracle gives the x86 answer on any host
+ * (AArch64 prefers signalling NaNs and returns a positive default NaN). */
+static inline float nan_rule32(float a, float b) {
+    if (a != a) return f32_of(f32_bits(a) | 0x00400000u);
+    if (b != b) return f32_of(f32_bits(b) | 0x00400000u);
+    return f32_of(0xFFC00000u);
+}
+static inline double nan_rule64(double a, double b) {
+    if (a != a) return f64_of(f64_bits(a) | 0x0008000000000000ull);
+    if (b != b) return f64_of(f64_bits(b) | 0x0008000000000000ull);
+    return f64_of(0xFFF8000000000000ull);
+}
+static inline float fsub32(float a, float b) { float r = a - b; return r == r ? r : nan_rule32(a, b); }
+static inline float fadd32(float a, float b) { float r = a + b; return r == r ? r : nan_rule32(a, b); }
+static inline float fmul32(float a, float b) { float r = a * b; return r == r ? r : nan_rule32(a, b); }
+static inline float fdiv32(float a, float b) { float r = a / b; return r == r ? r : nan_rule32(a, b); }
+static inline double fsub64(double a, double b) { double r = a - b; return r == r ? r : nan_rule64(a, b); }
+static inline double fadd64(double a, double b) { double r = a + b; return r == r ? r : nan_rule64(a, b); }
+static inline double fmul64(double a, double b) { double r = a * b; return r == r ? r : nan_rule64(a, b); }
+static inline double fdiv64(double a, double b) { double r = a / b; return r == r ? r : nan_rule64(a, b); }
+/* cvtsd2ss / cvtss2sd on NaN: top mantissa bits kept, quiet bit set. */
+static inline float d2f(double d) {
+    if (d == d) return (float)d;
+    uint64_t b = f64_bits(d);
+    return f32_of((uint32_t)(b >> 32 & 0x80000000u) | 0x7FC00000u | (uint32_t)(b >> 29 & 0x7FFFFFu));
+}
+static inline double f2d(float f) {
+    if (f == f) return (double)f;
+    uint32_t b = f32_bits(f);
+    return f64_of(((uint64_t)(b & 0x80000000u) << 32) | 0x7FF8000000000000ull | ((uint64_t)(b & 0x7FFFFFu) << 29));
+}
+
 /* Big-endian field helpers: floatToBytes / bytesToFloat and sizeToBytes /
  * bytesToLong_bigEndian, szx/src/szx_BytesToolkit.cc:266-317,460-476,805-814. */
 static void put_be32(uint8_t* p, uint32_t v) {
@@ -101,8 +137,8 @@ float orc_value_range_f32(const float* x, size_t n, float* radius, float* median
         if (mn > v) mn = v;
         else if (mx < v) mx = v;
     }
-    float range = mx - mn;
-    if (radius) { *radius = range / 2; *median = mn + *radius; }
+    float range = fsub32(mx, mn);
+    if (radius) { *radius = fdiv32(range, 2); *median = fadd32(mn, *radius); }
     return range;
 }
 
@@ -115,8 +151,8 @@ double orc_value_range_f64(const double* x, size_t n, float* radius, float* medi
         if (mn > v) mn = v;
         else if (mx < v) mx = v;
     }
-    double range = mx - mn;
-    if (radius) { *radius = (float)(range / 2); *median = (float)(mn + (double)*radius); }
+    double range = fsub64(mx, mn);
+    if (radius) { *radius = d2f(fdiv64(range, 2)); *median = d2f(fadd64(mn, f2d(*radius))); }
     return range;
 }
 
@@ -130,10 +166,10 @@ static int stats_block_f32(const float* x, size_t n, float eb, float* median, fl
         if (mn > v) mn = v;
         else if (mx < v) mx = v;
     }
-    float range = mx - mn;
-    float r = range / 2;
+    float range = fsub32(mx, mn);
+    float r = fdiv32(range, 2);
     *radius = r;
-    *median = mn + r;
+    *median = fadd32(mn, r);
     return r <= eb ? 0 : 1;
 }
 
@@ -146,11 +182,11 @@ static int stats_block_f64(const double* x, size_t n, float eb, float* median, f
         if (mn > v) mn = v;
         else if (mx < v) mx = v;
     }
-    double range = mx - mn;
-    double r = range / 2;
-    double m = mn + r;
-    *radius = (float)r;
-    *median = (float)m;
+    double range = fsub64(mx, mn);
+    double r = fdiv64(range, 2);
+    double m = fadd64(mn, r);
+    *radius = d2f(r);
+    *median = d2f(m);
     return r <= (double)eb ? 0 : 1;
 }
 
@@ -162,9 +198,9 @@ static int stats_block_f64_omp(const double* x, size_t n, float eb, float* media
         if (x[j] > mx) mx = x[j];
         if (x[j] < mn) mn = x[j];
     }
-    double range = mx - mn;
-    *radius = (float)(range / 2);
-    *median = (float)(mn + (double)*radius);
+    double range = fsub64(mx, mn);
+    *radius = d2f(fdiv64(range, 2));
+    *median = d2f(fadd64(mn, f2d(*radius)));
     return *radius <= eb ? 0 : 1;
 }
 
@@ -197,7 +233,7 @@ static size_t enc_block_f32(const float* x, size_t n, float eb, float median, fl
     uint32_t prev = 0;
     size_t m = 0;
     for (size_t i = 0; i < n; i++) {
-        float d = x[i] - median;
+        float d = fsub32(x[i], median);
         uint32_t cur = f32_bits(d) >> s;
         int ld = lead_code32(cur ^ prev);
         lead[i >> 2] |= (uint8_t)(ld << (6 - 2 * (i & 3)));
@@ -213,7 +249,7 @@ static size_t enc_block_f32(const float* x, size_t n, float eb, float median, fl
  * The subtraction uses the float median widened to double (:38) even when the
  * stored median is zeroed by the reqLength clamp (:46, :421). */
 static size_t enc_block_f64(const double* x, size_t n, float eb, float mValue, float radius, uint8_t* out) {
-    double median = (double)mValue;
+    double median = f2d(mValue);
     int reqLength = reqlen_f64(eb, radius, &mValue);
     int R, s;
     split_reqlen(reqLength, &R, &s);
@@ -224,7 +260,7 @@ static size_t enc_block_f64(const double* x, size_t n, float eb, float mValue, f
     uint64_t prev = 0;
     size_t m = 0;
     for (size_t i = 0; i < n; i++) {
-        double d = x[i] - median;
+        double d = fsub64(x[i], median);
         uint64_t cur = f64_bits(d) >> s;
         int ld = lead_code64(cur ^ prev);
         lead[i >> 2] |= (uint8_t)(ld << (6 - 2 * (i & 3)));
@@ -259,7 +295,7 @@ static size_t dec_block_f32(const uint8_t* p, size_t n, float* out) {
             else cur |= (uint32_t)q[m++] << (8 * b);
         }
         uint32_t sh = cur << s;
-        out[i] = f32_of(sh) + median;
+        out[i] = fadd32(f32_of(sh), median);
         prev = sh >> s;
     }
     return 5 + L + m;
@@ -270,7 +306,7 @@ static size_t dec_block_f32(const uint8_t* p, size_t n, float* out) {
  * fourth stored byte instead of the fifth, as szxd_double.cc:244 does. */
 static size_t dec_block_f64(const uint8_t* p, size_t n, double* out, int ref_compat) {
     int reqLength = p[0];
-    double median = (double)f32_of(get_be32(p + 1));
+    double median = f2d(f32_of(get_be32(p + 1)));
     int R, s;
     split_reqlen(reqLength, &R, &s);
     size_t L = ceil_div(n, 4);
@@ -289,7 +325,7 @@ static size_t dec_block_f64(const uint8_t* p, size_t n, double* out, int ref_com
         if (ref_compat && R == 5 && ld == 0)
             cur = (cur & 0x00FFFFFFFFFFFFFFull) | ((uint64_t)q[m0 + 3] << 56);
         uint64_t sh = cur << s;
-        out[i] = f64_of(sh) + median;
+        out[i] = fadd64(f64_of(sh), median);
         prev = sh >> s;
     }
     return 5 + L + m;
@@ -413,10 +449,10 @@ size_t orc_fast_compress_args(int fastMode, int dt, const void* data, size_t n, 
          * narrowed to float); the non-blocked branch :279-285 does the same. */
         if (dt == ORC_FLOAT) {
             float range = orc_value_range_f32((const float*)data, n, NULL, NULL);
-            eb = range * rel;
+            eb = fmul32(range, rel);
         } else {
             double range = orc_value_range_f64((const double*)data, n, NULL, NULL);
-            eb = (float)(range * rel);
+            eb = d2f(fmul64(range, f2d(rel)));
         }
     }
     return orc_compress(fastMode, dt, data, n, eb, bs, out, cap);
@@ -464,7 +500,7 @@ static int decompress_blocked(int mode, int dt, const uint8_t* s, size_t len, si
             float m = mode == 4 ? f32_of(get_le32(p + 4 * j)) : f32_of(get_be32(p + 4 * j));
             j++;
             if (dt == ORC_FLOAT) for (size_t e = 0; e < blen; e++) ((float*)outv)[off + e] = m;
-            else for (size_t e = 0; e < blen; e++) ((double*)outv)[off + e] = (double)m;
+            else for (size_t e = 0; e < blen; e++) ((double*)outv)[off + e] = f2d(m);
         }
     }
     return 0;
@@ -578,7 +614,7 @@ int orc_decompress_m3_omp(int dt, const uint8_t* s, size_t len, size_t n, void* 
         } else {
             float m = f32_of(get_be32(P + 4 * ((size_t)b - rank[b])));
             if (dt == ORC_FLOAT) for (size_t e = 0; e < blen; e++) ((float*)out)[off + e] = m;
-            else for (size_t e = 0; e < blen; e++) ((double*)out)[off + e] = (double)m;
+            else for (size_t e = 0; e < blen; e++) ((double*)out)[off + e] = f2d(m);
         }
     }
     free(pos); free(rank);
@@ -609,7 +645,7 @@ static float fxr_cr(const float* x, size_t n, int bs, int rate, const float* rad
         uint32_t prev = 0;
         int acc = 0;
         for (int j = 0; j < bs; j++) {
-            float dv = d[j] - median;
+            float dv = fsub32(d[j], median);
             uint32_t cur = f32_bits(dv) >> s;
             int ld = lead_code32(cur ^ prev);
             acc += ld >= R ? R : ld;
@@ -639,11 +675,11 @@ static void fxr_sample(const float* x, size_t n, int bs, int rate, float** rads,
         }
         if (gmax < mx) gmax = mx;
         if (gmin > mn) gmin = mn;
-        float r = (mx - mn) / 2;
+        float r = fdiv32(fsub32(mx, mn), 2);
         (*rads)[i] = r;
-        (*meds)[i] = mn + r;
+        (*meds)[i] = fadd32(mn, r);
     }
-    *range = gmax - gmin;
+    *range = fsub32(gmax, gmin);
 }
 
 float orc_fxr_estimate_cr_f32(const float* x, size_t n, int bs, float eb, size_t* sumReq, size_t* sumLead) {

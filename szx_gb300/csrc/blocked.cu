@@ -172,6 +172,7 @@ struct EncArgs {
     const void* x;
     unsigned long long n, nb, ntiles;
     int bs;
+    int omp_stats;               // mode-4 double statistics
     float eb;
     const CodecParams* params;   // when set, params->eb overrides eb
     uint8_t* payload;            // fixed position of the payload region
@@ -201,7 +202,8 @@ struct BlockEnc {
 
 // Stats + shifted words + lead codes of one block (pass A).
 template <typename T, int E>
-__device__ __forceinline__ BlockEnc enc_block_a(const T* __restrict__ xb, int len, float eb, LaneEnc<T, E>& L) {
+__device__ __forceinline__ BlockEnc enc_block_a(const T* __restrict__ xb, int len, float eb, bool omp_stats,
+                                                LaneEnc<T, E>& L) {
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
@@ -215,18 +217,25 @@ __device__ __forceinline__ BlockEnc enc_block_a(const T* __restrict__ xb, int le
     BlockEnc B;
     float radius_f, median_f;
     if constexpr (sizeof(T) == 4) {
-        float range = __fsub_rn(mx, mn);
-        radius_f = __fdiv_rn(range, 2.0f);
-        median_f = __fadd_rn(mn, radius_f);
+        float range = xsub(mx, mn);
+        radius_f = xdiv(range, 2.0f);
+        median_f = xadd(mn, radius_f);
         B.state = (radius_f <= eb) ? 0 : 1;
-    } else {
+    } else if (!omp_stats) {
         // szx/src/szx_double.cc:991-1003: double statistics, float median/radius
-        double range = __dsub_rn(mx, mn);
-        double radius = __ddiv_rn(range, 2.0);
-        double median = __dadd_rn(mn, radius);
+        double range = xsub(mx, mn);
+        double radius = xdiv(range, 2.0);
+        double median = xadd(mn, radius);
         B.state = (radius <= (double)eb) ? 0 : 1;
-        radius_f = __double2float_rn(radius);
-        median_f = __double2float_rn(median);
+        radius_f = xd2f(radius);
+        median_f = xd2f(median);
+    } else {
+        // OpenMP layout, computeStateMedianRadius_double2 (szx/src/szx_double.cc:1120-1135):
+        // the median is formed from the float-rounded radius, compared in float
+        double range = xsub(mx, mn);
+        radius_f = xd2f(xdiv(range, 2.0));
+        median_f = xd2f(xadd(mn, xf2d(radius_f)));
+        B.state = (radius_f <= eb) ? 0 : 1;
     }
     B.med_bits = __float_as_uint(median_f);
     B.size = 0;
@@ -243,9 +252,20 @@ __device__ __forceinline__ BlockEnc enc_block_a(const T* __restrict__ xb, int le
     // the float median widened, even when the stored one is zeroed (szx_double.cc:38)
     T med;
     if constexpr (sizeof(T) == 4) med = zm ? 0.0f : median_f;
-    else med = (double)median_f;
+    else med = xf2d(median_f);
+    T d[E];
+    bool bad = false;
 #pragma unroll
-    for (int e = 0; e < E; e++) L.cur[e] = EL::bits(EL::sub(v[e], med)) >> s;
+    for (int e = 0; e < E; e++) {
+        d[e] = EL::sub(v[e], med);
+        bad |= d[e] != d[e];
+    }
+    if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+        for (int e = 0; e < E; e++) d[e] = xsub(v[e], med);
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) L.cur[e] = EL::bits(d[e]) >> s;
     U prev = __shfl_up_sync(0xffffffffu, L.cur[E - 1], 1);
     if (lane == 0) prev = 0;
 #pragma unroll
@@ -403,7 +423,7 @@ __global__ void __launch_bounds__(kEncThreads) k_blocked_encode(EncArgs a) {
                 unsigned long long off = b * (unsigned long long)a.bs;
                 unsigned long long rem = a.n - off;
                 len = rem < (unsigned long long)a.bs ? (int)rem : a.bs;
-                B[k] = enc_block_a<T, E>(x + off, len, eb, L[k]);
+                B[k] = enc_block_a<T, E>(x + off, len, eb, a.omp_stats, L[k]);
             } else {
                 B[k].state = 2;
                 B[k].size = 0;
@@ -555,6 +575,7 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
     if ((e = cudaMemsetAsync(ws.err, 0, sizeof(int), s)) != cudaSuccess) return e;
     EncArgs a;
     a.x = x; a.n = n; a.nb = nb; a.ntiles = ntiles; a.bs = bs; a.eb = abs_eb;
+    a.omp_stats = layout == kRandomAccessNative;
     a.params = use_params ? ws.params : nullptr;
     a.payload = d_out + qfix;
     a.payload_cap = cap - qfix;
@@ -807,14 +828,22 @@ __device__ __forceinline__ void dec_block(const uint8_t* p, int len, T* outb) {
     uint32_t ex = __shfl_up_sync(0xffffffffu, sum, 1);
     if (lane == 0) ex = 0;   // previous value at block start is zero
     U prev = (U)(ex & 0xFFFFFFu) << TOPSH;
+    const T med = widen_median<T>(med_f);
     T v[E];
+    bool bad = false;
 #pragma unroll
     for (int e = 0; e < E; e++) {
         int ld = (codes >> (2 * (E - 1 - e))) & 3;
         U inh = ld ? ~(((U)1 << (8 * (W - ld))) - 1) : (U)0;       // top `ld` bytes come from prev
         U cur = sp[e] | (prev & inh);
-        v[e] = EL::add(EL::of(cur << s), (T)med_f);
+        sp[e] = cur << s;
+        v[e] = EL::add(EL::of(sp[e]), med);
+        bad |= v[e] != v[e];
         prev = cur;
+    }
+    if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = xadd(EL::of(sp[e]), med);
     }
     store_lane<T, E>(outb + lane * E, nv, lane_vec_ok<T, E>(outb), v);
 }
@@ -859,7 +888,7 @@ __global__ void __launch_bounds__(kDecThreads) k_blocked_decode(const uint8_t* _
             uint32_t mbits = native_medians
                                  ? ((uint32_t)mp[0] | ((uint32_t)mp[1] << 8) | ((uint32_t)mp[2] << 16) | ((uint32_t)mp[3] << 24))
                                  : (((uint32_t)mp[0] << 24) | ((uint32_t)mp[1] << 16) | ((uint32_t)mp[2] << 8) | mp[3]);
-            T m = (T)__uint_as_float(mbits);
+            T m = widen_median<T>(__uint_as_float(mbits));
             int nv = blen - lane * E;
             nv = nv < 0 ? 0 : (nv > E ? E : nv);
             T v[E];

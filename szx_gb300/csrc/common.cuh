@@ -41,6 +41,51 @@ template <> struct Elem<double> {
     static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 };
 
+// ------------------------------------------------------------------ x86 NaN rules
+//
+// The reference runs on x86-64 SSE, where an arithmetic NaN result is the
+// first NaN operand, quieted (the second when only it is NaN), an invalid
+// operation (inf - inf, 0/0) gives the negative "indefinite" NaN, and
+// float<->double conversions keep the payload.  CUDA returns one canonical
+// NaN instead.  These helpers restore the x86 result; the hot loops call the
+// plain operation and take the fix-up path only when a warp saw a NaN.
+__device__ __forceinline__ float nan_rule(float a, float b) {
+    uint32_t ua = __float_as_uint(a), ub = __float_as_uint(b);
+    if ((ua & 0x7FFFFFFFu) > 0x7F800000u) return __uint_as_float(ua | 0x00400000u);
+    if ((ub & 0x7FFFFFFFu) > 0x7F800000u) return __uint_as_float(ub | 0x00400000u);
+    return __uint_as_float(0xFFC00000u);
+}
+__device__ __forceinline__ double nan_rule(double a, double b) {
+    unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+    unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+    if ((ua & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return __longlong_as_double((long long)(ua | 0x0008000000000000ull));
+    if ((ub & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return __longlong_as_double((long long)(ub | 0x0008000000000000ull));
+    return __longlong_as_double((long long)0xFFF8000000000000ull);
+}
+__device__ __forceinline__ float xsub(float a, float b) { float r = __fsub_rn(a, b); return r == r ? r : nan_rule(a, b); }
+__device__ __forceinline__ float xadd(float a, float b) { float r = __fadd_rn(a, b); return r == r ? r : nan_rule(a, b); }
+__device__ __forceinline__ float xmul(float a, float b) { float r = __fmul_rn(a, b); return r == r ? r : nan_rule(a, b); }
+__device__ __forceinline__ float xdiv(float a, float b) { float r = __fdiv_rn(a, b); return r == r ? r : nan_rule(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { double r = __dsub_rn(a, b); return r == r ? r : nan_rule(a, b); }
+__device__ __forceinline__ double xadd(double a, double b) { double r = __dadd_rn(a, b); return r == r ? r : nan_rule(a, b); }
+__device__ __forceinline__ double xmul(double a, double b) { double r = __dmul_rn(a, b); return r == r ? r : nan_rule(a, b); }
+__device__ __forceinline__ double xdiv(double a, double b) { double r = __ddiv_rn(a, b); return r == r ? r : nan_rule(a, b); }
+// cvtsd2ss / cvtss2sd
+__device__ __forceinline__ float xd2f(double d) {
+    if (d == d) return __double2float_rn(d);
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return __uint_as_float((uint32_t)(b >> 32 & 0x80000000u) | 0x7FC00000u | (uint32_t)(b >> 29 & 0x7FFFFFu));
+}
+__device__ __forceinline__ double xf2d(float f) {
+    if (f == f) return (double)f;
+    uint32_t b = __float_as_uint(f);
+    return __longlong_as_double((long long)(((unsigned long long)(b & 0x80000000u) << 32) | 0x7FF8000000000000ull |
+                                            ((unsigned long long)(b & 0x7FFFFFu) << 29)));
+}
+template <typename T> __device__ __forceinline__ T widen_median(float m);
+template <> __device__ __forceinline__ float widen_median<float>(float m) { return m; }
+template <> __device__ __forceinline__ double widen_median<double>(float m) { return xf2d(m); }
+
 // getExponent_float / getPrecisionReqLength_double, szx/src/szx_BytesToolkit.cc:335-387
 __device__ __forceinline__ int exponent_f32(float v) { return (int)((__float_as_uint(v) & 0x7F800000u) >> 23) - 127; }
 __device__ __forceinline__ int exponent_f64_of_f32(float v) {

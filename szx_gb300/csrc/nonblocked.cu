@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
     split_reqlen(reqLength, &R, &s);
     T med;
     if constexpr (sizeof(T) == 4) med = zm ? 0.0f : P.median;
-    else med = (double)P.median;
+    else med = xf2d(P.median);
     const uint32_t med_stored = zm ? 0u : __float_as_uint(P.median);
     const unsigned long long L = (a.n + 3) / 4;
     uint8_t* lead = a.out + kNbShift + 17;
@@ -180,10 +180,19 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
         T v[kNbPer];
         load16<T>(x, first, a.n, v);
         U cur[kNbPer];
+        bool bad = false;
 #pragma unroll
-        for (int e = 0; e < kNbPer; e++) cur[e] = EL::bits(EL::sub(v[e], med)) >> s;
+        for (int e = 0; e < kNbPer; e++) {
+            T d = EL::sub(v[e], med);
+            bad |= d != d;
+            cur[e] = EL::bits(d) >> s;
+        }
+        if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+            for (int e = 0; e < kNbPer; e++) cur[e] = EL::bits(xsub(v[e], med)) >> s;
+        }
         U prev = __shfl_up_sync(0xffffffffu, cur[kNbPer - 1], 1);
-        if (lane == 0) prev = first > 0 && first - 1 < a.n ? (EL::bits(EL::sub(x[first - 1], med)) >> s) : (U)0;
+        if (lane == 0) prev = first > 0 && first - 1 < a.n ? (EL::bits(xsub(x[first - 1], med)) >> s) : (U)0;
         uint32_t codes = 0, mine = 0;
 #pragma unroll
         for (int e = 0; e < kNbPer; e++) {
@@ -416,7 +425,7 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_decode(const uint8_t* __restr
     const uint8_t* lead = s + 17;
     const uint8_t* mid = s + h.mid_off;
     const uint8_t* send = s + len;
-    const T med = (T)h.median;
+    const T med = widen_median<T>(h.median);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (;;) {
         if (threadIdx.x == 0) s_tile = (long long)atomicAdd(ctr, 1ull);
@@ -509,13 +518,20 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_decode(const uint8_t* __restr
         uint32_t full = lane ? comb(wpre, exs) : wpre;
         U prev = (U)(full & 0xFFFFFFu) << TOPSH;
         T v[kNbPer];
+        bool bad = false;
 #pragma unroll
         for (int e = 0; e < kNbPer; e++) {
             int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
             U inh = ld ? ~(((U)1 << (8 * (W - ld))) - 1) : (U)0;
             U cur = sp[e] | (prev & inh);
-            v[e] = EL::add(EL::of(cur << sft), med);
+            sp[e] = cur << sft;
+            v[e] = EL::add(EL::of(sp[e]), med);
+            bad |= v[e] != v[e];
             prev = cur;
+        }
+        if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+            for (int e = 0; e < kNbPer; e++) v[e] = xadd(EL::of(sp[e]), med);
         }
         store16<T>(out, first, h.n, v);
         __syncthreads();

@@ -193,12 +193,12 @@ __global__ void __launch_bounds__(kRangeThreads) k_range(const T* __restrict__ x
             if (mn == 0.0f) mn = x[f.z];
             if (mx == 0.0f) mx = x[f.z];
         }
-        float range = __fsub_rn(mx, mn);
+        float range = xsub(mx, mn);
         p.range_f = range;
-        p.range_d = (double)range;
-        p.radius = __fdiv_rn(range, 2.0f);
-        p.median = __fadd_rn(mn, p.radius);
-        p.eb = err_mode == 1 ? __fmul_rn(range, rel) : abs_eb;
+        p.range_d = xf2d(range);
+        p.radius = xdiv(range, 2.0f);
+        p.median = xadd(mn, p.radius);
+        p.eb = err_mode == 1 ? xmul(range, rel) : abs_eb;
     } else {
         double x0 = x[0];
         double mn, mx;
@@ -211,12 +211,12 @@ __global__ void __launch_bounds__(kRangeThreads) k_range(const T* __restrict__ x
                 if (mx == 0.0) mx = x[f.z];
             }
         }
-        double range = __dsub_rn(mx, mn);
+        double range = xsub(mx, mn);
         p.range_d = range;
-        p.range_f = (float)range;
-        p.radius = __double2float_rn(__ddiv_rn(range, 2.0));
-        p.median = __double2float_rn(__dadd_rn(mn, (double)p.radius));
-        p.eb = err_mode == 1 ? __double2float_rn(__dmul_rn(range, (double)rel)) : abs_eb;
+        p.range_f = xd2f(range);
+        p.radius = xd2f(xdiv(range, 2.0));
+        p.median = xd2f(xadd(mn, xf2d(p.radius)));
+        p.eb = err_mode == 1 ? xd2f(xmul(range, xf2d(rel))) : abs_eb;
     }
     *out = p;
 }

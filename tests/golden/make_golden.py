@@ -121,6 +121,18 @@ def cases():
         add(f"{tag}_zeros_m1", signed_zeros(rng, 3000, dt), 1, ABS, eb=1e-2)
         add(f"{tag}_allconst_m3", np.full(2000, 1.25, dt), 3, ABS, eb=1e-3)
         add(f"{tag}_ragged_n1025_m3", smooth_1d(rng, 1025, dt), 3, ABS, eb=1e-3)
+    # NaN / infinity inputs: pins the x86 NaN propagation of the reference
+    for dt, tag in ((np.float32, "f32"), (np.float64, "f64")):
+        base = np.sin(np.arange(3000) / 40.0).astype(dt)
+        x = base.copy(); x[0] = np.nan
+        add(f"{tag}_nan_first_m3", x, 3, ABS, eb=1e-2)
+        add(f"{tag}_nan_first_m1", x, 1, ABS, eb=1e-2)
+        x = base.copy(); x[300::257] = np.nan
+        add(f"{tag}_nan_inside_m3", x, 3, ABS, eb=1e-2)
+        add(f"{tag}_nan_inside_m1", x, 1, ABS, eb=1e-2)
+        x = base.copy(); x[130] = np.inf; x[140] = -np.inf; x[1000] = np.inf
+        add(f"{tag}_inf_m3", x, 3, ABS, eb=1e-2)
+        add(f"{tag}_inf_m1", x, 1, ABS, eb=1e-2)
     # reqLength clamp at 32 (float, median forced to 0) and at 64 (double)
     add("f32_clamp32_m3", offset_smooth(rng, 4000, np.float32, 1e6), 3, ABS, eb=1e-6)
     add("f32_clamp32_m1", offset_smooth(rng, 4000, np.float32, 1e6), 1, ABS, eb=1e-6)
