@@ -110,6 +110,7 @@ void SZx_fast_decompress_args_unpredictable_blocked(void* newData, int dataType,
 #define SZXG_ERR_ARG 4        /* invalid argument */
 #define SZXG_ERR_CUDA 5       /* CUDA runtime error */
 #define SZXG_ERR_UNSUPPORTED 6
+#define SZXG_ERR_TOO_LARGE 7      /* input beyond the fixed scratch of SZxG_compress_noalloc */
 
 int SZxG_get_last_error(void);
 const char* SZxG_error_string(int code);
@@ -144,6 +145,21 @@ int SZxG_decompress(int fastMode, int dataType, const void* d_stream, size_t str
 /* Read back the status a previous SZxG_* call left in its workspace (waits
  * for `stream`). */
 int SZxG_workspace_status(const void* d_workspace, void* stream);
+
+/* No counterpart in the reference.  SZxG_compress for the blocked layouts
+ * (fastMode 2, 3, 4) that allocates nothing: its scratch is a fixed array in
+ * device memory that every GPU loading this library holds until exit (about
+ * 7.7 MiB).  For callers that may not call cudaMalloc -- applications whose
+ * own pool allocator owns all device memory, or loops that cannot pay for
+ * cudaMalloc's device-wide synchronisation.  At most 1,048,576 blocks per
+ * call (ceil(nbEle/blockSize); 134,217,728 values at blockSize 128), else
+ * SZXG_ERR_TOO_LARGE before any GPU work.  All calls on a device share the
+ * array: calls that overlap on the GPU race, so order them on one stream.
+ * The first call on a device resolves the array's address; make it before
+ * any stream capture.  Output, info and errors as SZxG_compress. */
+int SZxG_compress_noalloc(int fastMode, int dataType, const void* d_data, size_t nbEle, int blockSize,
+                          int errBoundMode, float absErrBound, float relBoundRatio, void* d_out, size_t outCapacity,
+                          SZxG_StreamInfo* d_info, void* stream);
 
 /* Host-buffer codec with an explicit block size (same stream as Part 1). */
 unsigned char* SZxG_compress_host(int fastMode, int dataType, const void* data, size_t nbEle, int blockSize,

@@ -319,6 +319,7 @@ const char* SZxG_error_string(int code) {
         case SZXG_ERR_ARG: return "invalid argument";
         case SZXG_ERR_CUDA: return "CUDA runtime error";
         case SZXG_ERR_UNSUPPORTED: return "unsupported layout, type or block size";
+        case SZXG_ERR_TOO_LARGE: return "input larger than the fixed scratch of SZxG_compress_noalloc (1,048,576 blocks)";
         default: return "unknown error";
     }
 }
