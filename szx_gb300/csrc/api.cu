@@ -35,7 +35,7 @@ int sm_count() {
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct WsLayout {
-    size_t hdr, st, st2, partials, o, m, s, p, rw, aux, total;
+    size_t hdr, st32, st, st2, partials, o, m, s, p, rw, aux, total;
     size_t status_tiles, status2_tiles, blocks, words, aux_tiles;
 };
 
@@ -52,6 +52,7 @@ static WsLayout ws_layout(int layout, int dtype, size_t n, int bs) {
     L.aux_tiles = tiles_elem;
     size_t off = 0;
     L.hdr = off; off += 4096;
+    L.st32 = off; off += a256(4 * (L.status_tiles + 16));
     L.st = off; off += a256(3 * 8 * L.status_tiles);
     L.st2 = off; off += a256(3 * 8 * L.status2_tiles);
     L.partials = off; off += a256(4096 * 24);
@@ -79,6 +80,7 @@ Workspace ws_carve(void* base, int layout, int dtype, size_t n, int bs) {
     w.nhdr = (NonBlockedHdr*)(h + 320);
     w.err = (int*)(h + 448);
     w.counters = (unsigned long long*)(h + 512);
+    w.st32 = (uint32_t*)(b + L.st32);
     w.st_word = (unsigned long long*)(b + L.st);
     w.st_agg2 = w.st_word + L.status_tiles;
     w.st_inc2 = w.st_agg2 + L.status_tiles;

@@ -105,70 +105,97 @@ __device__ __forceinline__ bool lane_vec_ok(const void* block_base) {
     return ((uintptr_t)block_base % A) == 0;
 }
 
-// ------------------------------------------------------------------ block statistics
+// ------------------------------------------------------------------ segment helpers
+//
+// A block is handled by a segment of G lanes (G a power of two), each lane
+// holding E consecutive values (16 float / 8 double).  Reductions and scans
+// run inside segments with shuffle widths of G, so several blocks share one
+// warp instruction and the per-block work is replicated G times, not 32.
 
-// Warp-wide min/max of one block with the reference's sequential semantics
-// (szx/src/szx_float.cc:322-345): the first element reaching an extreme wins,
-// NaNs are skipped unless the block's first element is NaN.
-template <typename T, int E>
-__device__ __forceinline__ void block_minmax(const T (&v)[E], int nv, T& mn, T& mx);
+template <typename T> struct EncCfg;
+template <> struct EncCfg<float> { static constexpr int E = 16; };
+template <> struct EncCfg<double> { static constexpr int E = 8; };
 
-template <typename T, int E>
-__device__ __forceinline__ void block_minmax(const T (&v)[E], int nv, T& mn, T& mx) {
+template <int G, typename V>
+__device__ __forceinline__ V seg_sum(V v) {
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d, G);
+    return v;
+}
+template <int G, typename V>
+__device__ __forceinline__ V seg_inclusive_sum(V v) {
+    const int sl = (int)(lane_id() & (G - 1));
+#pragma unroll
+    for (int d = 1; d < G; d <<= 1) {
+        V o = __shfl_up_sync(0xffffffffu, v, d, G);
+        if (sl >= d) v += o;
+    }
+    return v;
+}
+
+// Segment-wide min/max with the reference's sequential semantics
+// (szx/src/szx_float.cc:322-345): the first value reaching an extreme wins,
+// NaNs are skipped unless the block's first value is NaN.
+template <typename T, int E, int G>
+__device__ __forceinline__ void seg_minmax(const T (&v)[E], int nv, T& mn, T& mx) {
     if constexpr (sizeof(T) == 4) {
-        float a = __int_as_float(0x7f800000), b = __int_as_float(0xff800000);
+        float lo = __builtin_huge_valf(), hi = -__builtin_huge_valf();
 #pragma unroll
         for (int e = 0; e < E; e++)
-            if (e < nv) { a = fminf(a, v[e]); b = fmaxf(b, v[e]); }
+            if (e < nv) { lo = fminf(lo, v[e]); hi = fmaxf(hi, v[e]); }
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) {
-            a = fminf(a, __shfl_xor_sync(0xffffffffu, a, d));
-            b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, d));
+        for (int d = G / 2; d > 0; d >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, d, G));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, d, G));
         }
-        mn = a;
-        mx = b;
+        mn = lo;
+        mx = hi;
     } else {
-        // order-preserving integer keys keep the FP64 pipe out of the reduction
-        long long a = 0x7FFFFFFFFFFFFFFFll, b = (long long)0x8000000000000000ull;
+        long long lo = 0x7FFFFFFFFFFFFFFFll, hi = (long long)0x8000000000000000ull;
 #pragma unroll
         for (int e = 0; e < E; e++) {
             unsigned long long u = (unsigned long long)__double_as_longlong(v[e]);
             bool ok = e < nv && (u & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
             long long k = (long long)(u ^ ((unsigned long long)((long long)u >> 63) & 0x7FFFFFFFFFFFFFFFull));
-            if (ok) { a = k < a ? k : a; b = k > b ? k : b; }
+            if (ok) { lo = k < lo ? k : lo; hi = k > hi ? k : hi; }
         }
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) {
-            long long oa = __shfl_xor_sync(0xffffffffu, a, d), ob = __shfl_xor_sync(0xffffffffu, b, d);
-            a = oa < a ? oa : a;
-            b = ob > b ? ob : b;
+        for (int d = G / 2; d > 0; d >>= 1) {
+            long long a = __shfl_xor_sync(0xffffffffu, lo, d, G), b = __shfl_xor_sync(0xffffffffu, hi, d, G);
+            lo = a < lo ? a : lo;
+            hi = b > hi ? b : hi;
         }
         auto inv = [](long long k) {
             unsigned long long u = (unsigned long long)k;
             return __longlong_as_double((long long)(u ^ ((unsigned long long)(k >> 63) & 0x7FFFFFFFFFFFFFFFull)));
         };
-        mn = inv(a);
-        mx = inv(b);
+        mn = inv(lo);
+        mx = inv(hi);
     }
-    T x0 = __shfl_sync(0xffffffffu, v[0], 0);
-    if (isnan(x0)) { mn = x0; mx = x0; return; }
-    if (mn == (T)0 || mx == (T)0) {
-        // a zero extreme keeps the sign of the first zero in the block
-        int ze = E;
-        T zv = 0;
+    // a zero extreme takes the sign of the block's first zero (all lanes take part)
+    int ze = E;
+    T zv = 0;
 #pragma unroll
-        for (int e = E - 1; e >= 0; e--)
-            if (e < nv && v[e] == (T)0) { ze = e; zv = v[e]; }
-        unsigned m = __ballot_sync(0xffffffffu, ze < E);
-        T first = __shfl_sync(0xffffffffu, zv, __ffs(m) - 1);
+    for (int e = E - 1; e >= 0; e--)
+        if (e < nv && v[e] == (T)0) { ze = e; zv = v[e]; }
+    const unsigned lane = lane_id();
+    const unsigned seg0 = lane & ~(unsigned)(G - 1);
+    const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
+    const unsigned m = __ballot_sync(0xffffffffu, ze < E) & segmask;
+    const int fl = m ? __ffs(m) - 1 : (int)seg0;
+    const T first = __shfl_sync(0xffffffffu, zv, fl);
+    if (m) {
         if (mn == (T)0) mn = first;
         if (mx == (T)0) mx = first;
     }
+    const T x0 = __shfl_sync(0xffffffffu, v[0], 0, G);
+    if (isnan(x0)) { mn = x0; mx = x0; }
 }
 
 // ------------------------------------------------------------------ encode
 
 struct EncArgs {
+    TileStatus32 st32;
     const void* x;
     unsigned long long n, nb, ntiles;
     int bs;
@@ -180,313 +207,358 @@ struct EncArgs {
     uint16_t* o_scr;
     uint32_t* m_scr;
     uint8_t* s_scr;
-    TileStatus st;
     unsigned long long* tile_ctr;
     int* err;
     Totals* tot;
 };
 
-template <typename T, int E>
-struct LaneEnc {
-    typename Elem<T>::U cur[E];
-    uint32_t codes;       // 2 bits per element, MSB-first
-    uint32_t lane_bytes;  // mid bytes this lane emits
+template <typename T, int G>
+struct EncTile {
+    static constexpr int E = EncCfg<T>::E;
+    static constexpr int kBsMax = G * E;                               // largest block of this variant
+    static constexpr int kBpw = 32 / G;                                // blocks per warp step
+    static constexpr int kRaw = 16384 / (kBsMax * (int)sizeof(T));
+    static constexpr int kBlocks = kRaw >= 64 ? 64 : (kRaw < 8 ? 8 : kRaw);   // blocks per tile
+    static constexpr int kIn = kBlocks * kBsMax * (int)sizeof(T);      // input bytes per stage
+    static constexpr int kMaxPay = 5 + (kBsMax + 3) / 4 + (int)sizeof(T) * kBsMax;
+    static constexpr int kStage = ((kBlocks * kMaxPay + 32 + 15) / 16) * 16;
+    static constexpr int kDynSmem = 3 * kIn + kStage;
+    static constexpr int kSlots = kBlocks * G;                         // (block, lane) slots per tile
 };
 
-struct BlockEnc {
-    int state;            // 0 constant, 1 non-constant, 2 absent
-    int reqLength;
-    uint32_t med_bits;    // median as stored
-    uint32_t size;        // payload bytes (non-constant)
-};
-
-// Stats + shifted words + lead codes of one block (pass A).
-template <typename T, int E>
-__device__ __forceinline__ BlockEnc enc_block_a(const T* __restrict__ xb, int len, float eb, bool omp_stats,
-                                                LaneEnc<T, E>& L) {
-    using EL = Elem<T>;
-    using U = typename EL::U;
-    constexpr int W = EL::W;
-    const int lane = (int)lane_id();
-    int nv = len - lane * E;
-    nv = nv < 0 ? 0 : (nv > E ? E : nv);
-    T v[E];
-    load_lane<T, E>(xb + lane * E, nv, lane_vec_ok<T, E>(xb) , v);
-    T mn, mx;
-    block_minmax<T, E>(v, nv, mn, mx);
-    BlockEnc B;
-    float radius_f, median_f;
-    if constexpr (sizeof(T) == 4) {
-        float range = xsub(mx, mn);
-        radius_f = xdiv(range, 2.0f);
-        median_f = xadd(mn, radius_f);
-        B.state = (radius_f <= eb) ? 0 : 1;
-    } else if (!omp_stats) {
-        // szx/src/szx_double.cc:991-1003: double statistics, float median/radius
-        double range = xsub(mx, mn);
-        double radius = xdiv(range, 2.0);
-        double median = xadd(mn, radius);
-        B.state = (radius <= (double)eb) ? 0 : 1;
-        radius_f = xd2f(radius);
-        median_f = xd2f(median);
-    } else {
-        // OpenMP layout, computeStateMedianRadius_double2 (szx/src/szx_double.cc:1120-1135):
-        // the median is formed from the float-rounded radius, compared in float
-        double range = xsub(mx, mn);
-        radius_f = xd2f(xdiv(range, 2.0));
-        median_f = xd2f(xadd(mn, xf2d(radius_f)));
-        B.state = (radius_f <= eb) ? 0 : 1;
-    }
-    B.med_bits = __float_as_uint(median_f);
-    B.size = 0;
-    B.reqLength = 0;
-    L.codes = 0;
-    L.lane_bytes = 0;
-    if (B.state == 0) return B;
-    bool zm;
-    B.reqLength = req_length<T>(eb, radius_f, &zm);
-    int R, s;
-    split_reqlen(B.reqLength, &R, &s);
-    if (zm) B.med_bits = 0;
-    // float data subtracts the (possibly zeroed) median; double data subtracts
-    // the float median widened, even when the stored one is zeroed (szx_double.cc:38)
-    T med;
-    if constexpr (sizeof(T) == 4) med = zm ? 0.0f : median_f;
-    else med = xf2d(median_f);
-    T d[E];
-    bool bad = false;
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-        d[e] = EL::sub(v[e], med);
-        bad |= d[e] != d[e];
-    }
-    if (__any_sync(0xffffffffu, bad)) {
-#pragma unroll
-        for (int e = 0; e < E; e++) d[e] = xsub(v[e], med);
-    }
-#pragma unroll
-    for (int e = 0; e < E; e++) L.cur[e] = EL::bits(d[e]) >> s;
-    U prev = __shfl_up_sync(0xffffffffu, L.cur[E - 1], 1);
-    if (lane == 0) prev = 0;
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-        U xr = L.cur[e] ^ (e ? L.cur[e - 1] : prev);
-        int lz;
-        if constexpr (sizeof(T) == 4) lz = __clz(xr) >> 3;
-        else lz = __clzll((long long)xr) >> 3;
-        int ld = lz < 3 ? lz : 3;
-        int cnt = R - ld;
-        cnt = cnt > 0 ? cnt : 0;
-        if (e < nv) {
-            L.codes |= (uint32_t)ld << (2 * (E - 1 - e));
-            L.lane_bytes += cnt;
-        }
-    }
-    uint32_t total = warp_sum(L.lane_bytes);
-    B.size = 5 + (uint32_t)((len + 3) / 4) + total;
-    (void)W;
-    return B;
-}
-
-// OR `cnt` bytes of `ev` into 32-bit words of a zeroed shared buffer at byte q.
-__device__ __forceinline__ void or_bytes(uint32_t* buf, uint32_t q, uint32_t ev, int cnt) {
-    if (cnt <= 0) return;
-    uint32_t sh = (q & 3) * 8;
-    uint32_t* w = buf + (q >> 2);
-    atomicOr(w, ev << sh);
-    if ((int)(q & 3) + cnt > 4) atomicOr(w + 1, ev >> (32 - sh));
-}
-__device__ __forceinline__ void or_bytes(uint32_t* buf, uint32_t q, unsigned long long ev, int cnt) {
-    if (cnt <= 0) return;
-    uint32_t sh = (q & 3) * 8;
-    uint32_t* w = buf + (q >> 2);
-    unsigned long long lo = ev << sh;
-    atomicOr(w, (uint32_t)lo);
-    int span = (int)(q & 3) + cnt;
-    if (span > 4) atomicOr(w + 1, (uint32_t)(lo >> 32));
-    if (span > 8) atomicOr(w + 2, (uint32_t)(ev >> (64 - sh)));
-}
-
-// Copy n bytes from a 16-aligned shared buffer (payload at offset sh) to global
-// dst (with dst % 16 == sh) using aligned 16-byte stores for whole chunks.
-__device__ __forceinline__ void warp_copy_out(const uint8_t* stage, uint32_t sh, uint32_t n, uint8_t* dst) {
+// Copy [sh, sh+n) of a 16-aligned shared buffer to global dst (dst % 16 ==
+// sh) with the whole CTA: aligned 16-byte stores, byte stores at the ragged ends.
+__device__ __forceinline__ void cta_copy_out(const uint8_t* stage, uint32_t sh, uint32_t n, uint8_t* dst) {
     uint8_t* gbase = dst - sh;
-    uint32_t end = sh + n;
-    uint32_t nch = (end + 15) >> 4;
-    for (uint32_t c = lane_id(); c < nch; c += 32) {
-        uint32_t lo = c << 4, hi = lo + 16;
-        if (lo >= sh && hi <= end) {
-            *(uint4*)(gbase + lo) = *(const uint4*)(stage + lo);
-        } else {
-            uint32_t a = lo > sh ? lo : sh, b = hi < end ? hi : end;
-            for (uint32_t j = a; j < b; j++) gbase[j] = stage[j];
-        }
+    const uint32_t end = sh + n, nch = (end + 15) >> 4;
+    for (uint32_t c = threadIdx.x; c < nch; c += blockDim.x) {
+        const uint32_t lo = c << 4;
+        if (lo >= sh && lo + 16 <= end) *(uint4*)(gbase + lo) = *(const uint4*)(stage + lo);
+    }
+    if (threadIdx.x < 32) {
+        const uint32_t last = nch - 1;
+        const uint32_t c = threadIdx.x < 16 ? 0 : last;
+        const bool part = threadIdx.x < 16 ? (sh > 0 || end < 16) : (last > 0 && (end & 15) != 0);
+        const uint32_t b = (c << 4) + (threadIdx.x & 15);
+        if (part && b >= sh && b < end) gbase[b] = stage[b];
     }
 }
 
-// Emit one non-constant block's payload (pass B).
-template <typename T, int E>
-__device__ __forceinline__ void enc_block_b(uint8_t* stage, uint8_t* dst, int len, const BlockEnc& B,
-                                            const LaneEnc<T, E>& L) {
+// One pass over the input, software-pipelined over three tile buffers:
+//   load tile t+2 (TMA bulk copy)  |  pass A of tile t+1, publish its aggregate
+//                                  |  resolve tile t's prefix, pass B of tile t
+// Pass A (a segment per block): statistics, state, reqLength, the shifted
+// words (written back over the input in shared memory), lead codes and
+// stored-byte counts.  Pass B emits the payloads of the whole tile into one
+// staging buffer with byte stores; the CTA then writes the tile's contiguous
+// byte range with aligned 16-byte stores.  Publishing tile t+1's aggregate
+// before resolving tile t means predecessors have normally published long
+// before a tile's look-back walks over them.
+template <typename T, int G>
+__global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
+    using TL = EncTile<T, G>;
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
-    const int lane = (int)lane_id();
-    const uint32_t sh = (uint32_t)((uintptr_t)dst & 15);
-    const uint32_t span = sh + B.size;
-    const uint32_t nz = (span + 16 + 15) >> 4;
-    for (uint32_t i = lane; i < nz; i += 32) ((uint4*)stage)[i] = make_uint4(0, 0, 0, 0);
-    __syncwarp();
-    uint8_t* p = stage + sh;
-    int R, s;
-    split_reqlen(B.reqLength, &R, &s);
-    const int Lb = (len + 3) / 4;
-    if (lane == 0) {
-        p[0] = (uint8_t)B.reqLength;
-        p[1] = (uint8_t)(B.med_bits >> 24);
-        p[2] = (uint8_t)(B.med_bits >> 16);
-        p[3] = (uint8_t)(B.med_bits >> 8);
-        p[4] = (uint8_t)B.med_bits;
-    }
-    // lead codes: 4 per byte, MSB first (szx/src/szx_TypeManager.cc:198-273)
-    if constexpr (E == 4) {
-        if (lane < Lb) p[5 + lane] = (uint8_t)L.codes;
-    } else if constexpr (E == 8) {
-        if (2 * lane < Lb) p[5 + 2 * lane] = (uint8_t)(L.codes >> 8);
-        if (2 * lane + 1 < Lb) p[6 + 2 * lane] = (uint8_t)L.codes;
-    } else if constexpr (E == 2) {
-        uint32_t nb = __shfl_down_sync(0xffffffffu, L.codes, 1);
-        if ((lane & 1) == 0 && lane / 2 < Lb) p[5 + lane / 2] = (uint8_t)((L.codes << 4) | nb);
-    } else {
-        uint32_t c1 = __shfl_down_sync(0xffffffffu, L.codes, 1);
-        uint32_t c2 = __shfl_down_sync(0xffffffffu, L.codes, 2);
-        uint32_t c3 = __shfl_down_sync(0xffffffffu, L.codes, 3);
-        if ((lane & 3) == 0 && lane / 4 < Lb) p[5 + lane / 4] = (uint8_t)((L.codes << 6) | (c1 << 4) | (c2 << 2) | c3);
-    }
-    // mid bytes: bytes [W-R .. W-1-lead] of each shifted word, ascending
-    uint32_t incl = warp_inclusive_sum(L.lane_bytes);
-    uint32_t q = sh + 5 + Lb + (incl - L.lane_bytes);
-    uint32_t* buf = (uint32_t*)stage;
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-        int ld = (L.codes >> (2 * (E - 1 - e))) & 3;
-        int cnt = R - ld;
-        if (lane * E + e < len && cnt > 0) {
-            U ev = L.cur[e] >> (8 * (W - R));
-            if constexpr (sizeof(T) == 4) {
-                ev &= cnt >= 4 ? 0xFFFFFFFFu : ((1u << (8 * cnt)) - 1);
-                or_bytes(buf, q, (uint32_t)ev, cnt);
-            } else {
-                ev &= cnt >= 8 ? ~0ull : ((1ull << (8 * cnt)) - 1);
-                or_bytes(buf, q, (unsigned long long)ev, cnt);
-            }
-            q += cnt;
-        }
-    }
-    __syncwarp();
-    warp_copy_out(stage, sh, B.size, dst);
-    __syncwarp();
-}
-
-template <typename T, int E>
-constexpr int enc_stage_bytes() {
-    return ((16 + 5 + (32 * E + 3) / 4 + (int)sizeof(T) * 32 * E + 32 + 15) / 16) * 16;
-}
-
-template <typename T, int E, int BPW>
-__global__ void __launch_bounds__(kEncThreads) k_blocked_encode(EncArgs a) {
-    constexpr int TB = kEncWarps * BPW;
-    static_assert(TB == 8 || TB == 16 || TB == 32, "tile of 8, 16 or 32 blocks");
-    constexpr int STAGE = enc_stage_bytes<T, E>();
-    __shared__ __align__(16) uint8_t s_stage[kEncWarps][STAGE];
-    __shared__ uint32_t s_size[TB], s_med[TB];
-    __shared__ int s_state[TB];
-    __shared__ unsigned long long s_off[TB];
-    __shared__ long long s_tile;
+    constexpr int E = TL::E;
+    constexpr int TB = TL::kBlocks;
+    constexpr int BPW = TL::kBpw;
+    constexpr int NGRP = TB / BPW;   // block groups per tile
+    extern __shared__ __align__(128) uint8_t dsm[];
+    uint8_t* bufs = dsm;
+    uint8_t* stg = dsm + 3 * TL::kIn;
+    __shared__ unsigned long long bar[3];
+    __shared__ uint32_t s_size[2][TB], s_med[2][TB], s_medf[2][TB], s_loc[2][TB], s_lrank[2][TB];
+    __shared__ uint8_t s_state[2][TB], s_req[2][TB];
+    __shared__ uint32_t s_codes[2][TL::kSlots];
+    __shared__ uint8_t s_lb[2][TL::kSlots];
+    __shared__ uint32_t s_agg[2][2];
+    __shared__ unsigned long long s_base;
+    __shared__ long long s_next;
     __shared__ int s_skip;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int seg = lane / G, sl = lane & (G - 1);
     const T* x = (const T*)a.x;
     const float eb = a.params ? a.params->eb : a.eb;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(a.tile_ctr, 1ull);
+    const long long nt = (long long)a.ntiles;
+    const unsigned long long tile_elems = (unsigned long long)TB * a.bs;
+    const bool tma_ok = ((uintptr_t)x & 15) == 0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 3; i++) mbar_init(&bar[i], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;   // bit i: parity to wait for on buffer i
+
+    auto tile_count = [&](long long t) {
+        const unsigned long long start = (unsigned long long)t * tile_elems;
+        const unsigned long long rem = a.n - start;
+        return rem < tile_elems ? rem : tile_elems;
+    };
+    auto issue = [&](long long t, int which) {
+        const unsigned long long cnt = tile_count(t);
+        const uint32_t bytes = (uint32_t)(cnt * sizeof(T));
+        const uint32_t tbytes = tma_ok ? (bytes & ~15u) : 0u;
+        T* dst = (T*)(bufs + which * TL::kIn);
+        const T* src = x + (unsigned long long)t * tile_elems;
+        if (threadIdx.x == 0 && tbytes) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(&bar[which], tbytes);
+            tma_load_1d(dst, src, tbytes, &bar[which]);
+        }
+        for (unsigned long long i = tbytes / sizeof(T) + threadIdx.x; i < cnt; i += kEncThreads) dst[i] = src[i];
+    };
+    auto wait_buf = [&](long long t, int which) {
+        if (tma_ok && ((tile_count(t) * sizeof(T)) & ~15ull)) {
+            if (!mbar_wait(&bar[which], (phase >> which) & 1u) && threadIdx.x == 0) atomicExch(a.err, kErrLookback);
+            phase ^= 1u << which;
+        }
+    };
+    auto acquire = [&]() {
         __syncthreads();
-        const long long tile = s_tile;
-        if (tile >= (long long)a.ntiles) break;
-        LaneEnc<T, E> L[BPW];
-        BlockEnc B[BPW];
-#pragma unroll
-        for (int k = 0; k < BPW; k++) {
-            const int lb = warp * BPW + k;
-            const unsigned long long b = (unsigned long long)tile * TB + lb;
+        if (threadIdx.x == 0) s_next = (long long)atomicAdd(a.tile_ctr, 1ull);
+        __syncthreads();
+        return s_next;
+    };
+
+    // ---- pass A of tile t held in buffer `which`, results in slot `sl2`;
+    // then warp 0 scans the tile and publishes its aggregate.
+    auto pass_a = [&](long long t, int which, int slot) {
+        T* xt = (T*)(bufs + which * TL::kIn);
+        for (int grp = warp; grp < NGRP; grp += kEncWarps) {
+            const int lb = grp * BPW + seg;
+            const unsigned long long b = (unsigned long long)t * TB + lb;
             int len = 0;
             if (b < a.nb) {
-                unsigned long long off = b * (unsigned long long)a.bs;
-                unsigned long long rem = a.n - off;
+                const unsigned long long rem = a.n - b * (unsigned long long)a.bs;
                 len = rem < (unsigned long long)a.bs ? (int)rem : a.bs;
-                B[k] = enc_block_a<T, E>(x + off, len, eb, a.omp_stats, L[k]);
-            } else {
-                B[k].state = 2;
-                B[k].size = 0;
-                B[k].med_bits = 0;
             }
-            if (lane == 0) {
-                s_size[lb] = B[k].state == 1 ? B[k].size : 0;
-                s_med[lb] = B[k].med_bits;
-                s_state[lb] = B[k].state;
+            T* xs = xt + (size_t)lb * a.bs;
+            int nv = len - sl * E;
+            nv = nv < 0 ? 0 : (nv > E ? E : nv);
+            T v[E];
+            load_lane<T, E>(xs + sl * E, nv, lane_vec_ok<T, E>(xs), v);
+            T mn, mx;
+            seg_minmax<T, E, G>(v, nv, mn, mx);
+            int state;
+            float radius_f, median_f;
+            if constexpr (sizeof(T) == 4) {
+                float range = xsub(mx, mn);
+                radius_f = xdiv(range, 2.0f);
+                median_f = xadd(mn, radius_f);
+                state = (radius_f <= eb) ? 0 : 1;
+            } else if (!a.omp_stats) {
+                // szx/src/szx_double.cc:991-1003: double statistics, float median/radius
+                double range = xsub(mx, mn);
+                double radius = xdiv(range, 2.0);
+                double median = xadd(mn, radius);
+                state = (radius <= (double)eb) ? 0 : 1;
+                radius_f = xd2f(radius);
+                median_f = xd2f(median);
+            } else {
+                // computeStateMedianRadius_double2 (szx/src/szx_double.cc:1120-1135)
+                double range = xsub(mx, mn);
+                radius_f = xd2f(xdiv(range, 2.0));
+                median_f = xd2f(xadd(mn, xf2d(radius_f)));
+                state = (radius_f <= eb) ? 0 : 1;
+            }
+            bool zm;
+            const int reqLength = req_length<T>(eb, radius_f, &zm);
+            int R, s;
+            split_reqlen(reqLength, &R, &s);
+            const uint32_t med_bits = zm ? 0u : __float_as_uint(median_f);
+            T med;
+            if constexpr (sizeof(T) == 4) med = __uint_as_float(med_bits);
+            else med = xf2d(median_f);
+            // shifted words, lead codes, stored-byte counts (szx/src/szx_float.cc:88-216)
+            T d[E];
+            bool bad = false;
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                d[e] = EL::sub(v[e], med);
+                bad |= d[e] != d[e];
+            }
+            if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+                for (int e = 0; e < E; e++) d[e] = xsub(v[e], med);
+            }
+            U cur[E];
+#pragma unroll
+            for (int e = 0; e < E; e++) cur[e] = EL::bits(d[e]) >> s;
+            U prev = __shfl_up_sync(0xffffffffu, cur[E - 1], 1, G);
+            if (sl == 0) prev = 0;
+            uint32_t codes = 0, lane_bytes = 0;
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                const U xr = cur[e] ^ (e ? cur[e - 1] : prev);
+                int lz;
+                if constexpr (sizeof(T) == 4) lz = __clz(xr | 0xFFu) >> 3;
+                else lz = __clzll((long long)(xr | 0xFFFFFFFFFFull)) >> 3;
+                const int c = R - lz;
+                if (e < nv) {
+                    codes |= (uint32_t)lz << (2 * (E - 1 - e));
+                    lane_bytes += c > 0 ? c : 0;
+                }
+            }
+            // keep the shifted words for pass B, over the input values
+            U* cs = (U*)(xs + sl * E);
+#pragma unroll
+            for (int e = 0; e < E; e++)
+                if (e < nv) cs[e] = cur[e];
+            s_codes[slot][lb * G + sl] = codes;
+            s_lb[slot][lb * G + sl] = (uint8_t)lane_bytes;
+            const uint32_t size = 5 + (uint32_t)((len + 3) / 4) + seg_sum<G>(lane_bytes);
+            if (sl == 0) {
+                const int st = len ? state : 2;
+                s_state[slot][lb] = (uint8_t)st;
+                s_size[slot][lb] = st == 1 ? size : 0;
+                s_med[slot][lb] = state == 1 ? med_bits : __float_as_uint(median_f);
+                s_medf[slot][lb] = __float_as_uint(median_f);
+                s_req[slot][lb] = (uint8_t)reqLength;
             }
         }
         __syncthreads();
         if (warp == 0) {
-            const bool in = lane < TB;
-            const int stt = in ? s_state[lane] : 2;
-            const uint32_t sz = in ? s_size[lane] : 0;
-            const uint32_t nn = stt == 1;
-            const uint32_t isz = warp_inclusive_sum(sz);
-            const uint32_t inn = warp_inclusive_sum(nn);
-            const uint32_t agg_sz = __shfl_sync(0xffffffffu, isz, 31);
-            const uint32_t agg_nn = __shfl_sync(0xffffffffu, inn, 31);
-            unsigned long long base_sz, base_nn;
-            lookback(a.st, tile, agg_sz, agg_nn, &base_sz, &base_nn, a.err);
-            const bool cap_ok = base_sz + agg_sz <= a.payload_cap;
-            if (in) s_off[lane] = base_sz + (isz - sz);
-            if (in && stt != 2) {
-                const unsigned long long b = (unsigned long long)tile * TB + lane;
-                const unsigned long long rank = base_nn + (inn - nn);
-                if (stt == 1) a.o_scr[rank] = (uint16_t)sz;
-                else a.m_scr[b - rank] = s_med[lane];
-            }
-            const uint32_t mask = __ballot_sync(0xffffffffu, in && stt == 1);
-            if (lane == 0) {
-                const uint32_t rev = __brev(mask);
-                if constexpr (TB == 32) *(uint32_t*)(a.s_scr + (unsigned long long)tile * 4) = bswap32(rev);
-                else {
+            const bool in0 = lane < TB, in1 = lane + 32 < TB;
+            const uint32_t sz0 = in0 ? s_size[slot][lane] : 0, sz1 = in1 ? s_size[slot][lane + 32] : 0;
+            const uint32_t nn0 = in0 && s_state[slot][lane] == 1, nn1 = in1 && s_state[slot][lane + 32] == 1;
+            const uint32_t i0 = warp_inclusive_sum(sz0), j0 = warp_inclusive_sum(nn0);
+            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), u0 = __shfl_sync(0xffffffffu, j0, 31);
+            const uint32_t i1 = warp_inclusive_sum(sz1) + t0, j1 = warp_inclusive_sum(nn1) + u0;
+            const uint32_t agg_sz = __shfl_sync(0xffffffffu, i1, 31), agg_nn = __shfl_sync(0xffffffffu, j1, 31);
+            if (in0) { s_loc[slot][lane] = i0 - sz0; s_lrank[slot][lane] = j0 - nn0; }
+            if (in1) { s_loc[slot][lane + 32] = i1 - sz1; s_lrank[slot][lane + 32] = j1 - nn1; }
+            if (lane == 0) { s_agg[slot][0] = agg_sz; s_agg[slot][1] = agg_nn; }
+            lookback_publish(a.st32, t, agg_sz, agg_nn);
+        }
+    };
+
+    // ---- warp 0: prefix of tile t (slot), per-block metadata
+    auto resolve = [&](long long t, int slot) {
+        if (warp != 0) return;
+        const uint32_t agg_sz = s_agg[slot][0], agg_nn = s_agg[slot][1];
+        unsigned long long base_sz, base_nn;
+        lookback_resolve(a.st32, t, agg_sz, agg_nn, &base_sz, &base_nn, a.err);
+        const bool cap_ok = base_sz + agg_sz <= a.payload_cap;
+        const unsigned long long tb0 = (unsigned long long)t * TB;
+        uint32_t m01[2];
 #pragma unroll
-                    for (int k = 0; k < TB / 8; k++)
-                        a.s_scr[(unsigned long long)tile * (TB / 8) + k] = (uint8_t)(rev >> (24 - 8 * k));
+        for (int h = 0; h < 2; h++) {
+            const int lb = lane + 32 * h;
+            const bool in = lb < TB;
+            const int st = in ? s_state[slot][lb] : 2;
+            if (in && st != 2) {
+                const unsigned long long rank = base_nn + s_lrank[slot][lb];
+                if (st == 1) a.o_scr[rank] = (uint16_t)s_size[slot][lb];
+                else a.m_scr[tb0 + lb - rank] = s_med[slot][lb];
+            }
+            m01[h] = __ballot_sync(0xffffffffu, in && st == 1);
+        }
+        if (lane == 0) {
+            // state bits, MSB first (szx/src/szx_TypeManager.cc:16-40)
+            uint8_t* sbp = a.s_scr + (unsigned long long)t * (TB / 8);
+            const uint32_t r0 = __brev(m01[0]), r1 = __brev(m01[1]);
+#pragma unroll
+            for (int k = 0; k < TB / 8; k++) sbp[k] = (uint8_t)((k < 4 ? r0 : r1) >> (24 - 8 * (k & 3)));
+            if (!cap_ok) atomicExch(a.err, kErrCapacity);
+            if (t == nt - 1) {
+                a.tot->payload_bytes = base_sz + agg_sz;
+                a.tot->nnc = base_nn + agg_nn;
+            }
+            s_base = base_sz;
+            s_skip = !cap_ok;
+        }
+    };
+
+    // ---- pass B of tile t: payloads into the staging buffer, then one copy-out
+    auto pass_b = [&](long long t, int which, int slot) {
+        const unsigned long long base = s_base;
+        const uint32_t sh = (uint32_t)((uintptr_t)(a.payload + base) & 15);
+        const T* xt = (const T*)(bufs + which * TL::kIn);
+        for (int grp = warp; grp < NGRP; grp += kEncWarps) {
+            const int lb = grp * BPW + seg;
+            const bool active = s_state[slot][lb] == 1;
+            const unsigned long long b = (unsigned long long)t * TB + lb;
+            int len = 0;
+            if (b < a.nb) {
+                const unsigned long long rem = a.n - b * (unsigned long long)a.bs;
+                len = rem < (unsigned long long)a.bs ? (int)rem : a.bs;
+            }
+            int nv = len - sl * E;
+            nv = nv < 0 ? 0 : (nv > E ? E : nv);
+            const int reqLength = s_req[slot][lb];
+            int R, s;
+            split_reqlen(reqLength, &R, &s);
+            (void)s;
+            const uint32_t codes = s_codes[slot][lb * G + sl];
+            const uint32_t lbytes = s_lb[slot][lb * G + sl];
+            const uint32_t incl = seg_inclusive_sum<G>(lbytes);
+            if (!active) continue;
+            uint8_t* p = stg + sh + s_loc[slot][lb];
+            const int Lb = (len + 3) / 4;
+            if (sl == 0) {
+                const uint32_t mb = s_med[slot][lb];
+                p[0] = (uint8_t)reqLength;
+                p[1] = (uint8_t)(mb >> 24);
+                p[2] = (uint8_t)(mb >> 16);
+                p[3] = (uint8_t)(mb >> 8);
+                p[4] = (uint8_t)mb;
+            }
+            // lead codes: 4 per byte, MSB first (szx/src/szx_TypeManager.cc:198-273)
+#pragma unroll
+            for (int j = 0; j < E / 4; j++) {
+                const int bi = sl * (E / 4) + j;
+                if (bi < Lb) p[5 + bi] = (uint8_t)(codes >> (8 * (E / 4 - 1 - j)));
+            }
+            // mid bytes: bytes [W-R .. W-1-lead] of each shifted word, ascending
+            uint8_t* q = p + 5 + Lb + (incl - lbytes);
+            const U* cs = (const U*)(xt + (size_t)lb * a.bs + sl * E);
+            const int low = 8 * (W - R);
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                if (e < nv) {
+                    const int ld = (codes >> (2 * (E - 1 - e))) & 3;
+                    const int c = R - ld;
+                    const U ev = cs[e] >> low;
+#pragma unroll
+                    for (int j = 0; j < W; j++)
+                        if (j < c) q[j] = (uint8_t)(ev >> (8 * j));
+                    q += c > 0 ? c : 0;
                 }
-                if (!cap_ok) atomicExch(a.err, kErrCapacity);
-                if (tile == (long long)a.ntiles - 1) {
-                    a.tot->payload_bytes = base_sz + agg_sz;
-                    a.tot->nnc = base_nn + agg_nn;
-                }
-                s_skip = !cap_ok;
             }
         }
         __syncthreads();
-        if (!s_skip) {
-#pragma unroll
-            for (int k = 0; k < BPW; k++) {
-                const int lb = warp * BPW + k;
-                if (B[k].state == 1) {
-                    const unsigned long long b = (unsigned long long)tile * TB + lb;
-                    const unsigned long long off = b * (unsigned long long)a.bs;
-                    const unsigned long long rem = a.n - off;
-                    const int len = rem < (unsigned long long)a.bs ? (int)rem : a.bs;
-                    enc_block_b<T, E>(s_stage[warp], a.payload + s_off[lb], len, B[k], L[k]);
-                }
-            }
-        }
+        if (!s_skip) cta_copy_out(stg, sh, s_agg[slot][0], a.payload + base);
+    };
+
+    // ---- pipeline
+    long long tb = acquire();
+    if (tb < nt) issue(tb, 0);
+    long long ta = acquire();
+    if (ta < nt) issue(ta, 1);
+    int ib = 0, slot = 0;
+    if (tb < nt) {
+        wait_buf(tb, 0);
         __syncthreads();
+        pass_a(tb, 0, 0);
+    }
+    while (tb < nt) {
+        const long long tn = acquire();
+        const int in_ = (ib + 2) % 3, ia = (ib + 1) % 3;
+        if (tn < nt) issue(tn, in_);
+        if (ta < nt) {
+            wait_buf(ta, ia);
+            __syncthreads();
+            pass_a(ta, ia, slot ^ 1);
+        }
+        resolve(tb, slot);
+        __syncthreads();
+        pass_b(tb, ib, slot);
+        tb = ta;
+        ta = tn;
+        ib = ia;
+        slot ^= 1;
     }
 }
 
@@ -551,10 +623,23 @@ size_t blocked_bound(int layout, int dtype, size_t n, int bs) {
     return hdr + sb + 4 * nb + nb * (5 + ((size_t)bs + 3) / 4) + es * n + 64;
 }
 
-template <typename T, int E, int BPW>
-static cudaError_t run_encode(const EncArgs& a, int grid, cudaStream_t s) {
+template <typename T, int G>
+static cudaError_t run_encode(EncArgs a, cudaStream_t s) {
+    using TL = EncTile<T, G>;
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(k_blocked_encode<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             TL::kDynSmem);
+        if (e != cudaSuccess) return e;
+        attr_set[dev] = true;
+    }
+    a.ntiles = (a.nb + TL::kBlocks - 1) / TL::kBlocks;
+    const size_t g = (size_t)sm_count() * 3;
+    const int grid = (int)(a.ntiles < g ? a.ntiles : g);
     TraceScope tr("blocked_encode", s);
-    k_blocked_encode<T, E, BPW><<<grid, kEncThreads, 0, s>>>(a);
+    k_blocked_encode<T, G><<<grid, kEncThreads, TL::kDynSmem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -562,41 +647,48 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
                                   float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s) {
     if (n == 0 || bs < 1 || bs > 256) return cudaErrorInvalidValue;
     if (layout == kBlocked && bs > 255) return cudaErrorInvalidValue;
-    const int E = bs <= 32 ? 1 : bs <= 64 ? 2 : bs <= 128 ? 4 : 8;
-    const int TB = E == 8 ? 16 : 32;
     const size_t nb = (n + bs - 1) / bs, sb = (nb + 7) / 8;
-    const size_t ntiles = (nb + TB - 1) / TB;
     const size_t hdr = layout == kBlocked ? 13 : 20;
     const size_t qfix = hdr + sb + 4 * nb;
     if (cap < qfix) return cudaErrorInvalidValue;
+    // tiles hold >= 8 blocks, so nb / 8 + 1 status words cover every tile size
+    const size_t max_tiles = nb / 8 + 1;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(ws.st_word, 0, sizeof(unsigned long long) * ntiles, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ws.st32, 0, sizeof(uint32_t) * (max_tiles + 8), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ws.counters, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ws.err, 0, sizeof(int), s)) != cudaSuccess) return e;
     EncArgs a;
-    a.x = x; a.n = n; a.nb = nb; a.ntiles = ntiles; a.bs = bs; a.eb = abs_eb;
+    a.st32 = TileStatus32{ws.st32, ws.st_agg2, ws.st_inc2};
+    a.x = x; a.n = n; a.nb = nb; a.ntiles = 0; a.bs = bs; a.eb = abs_eb;
     a.omp_stats = layout == kRandomAccessNative;
     a.params = use_params ? ws.params : nullptr;
     a.payload = d_out + qfix;
     a.payload_cap = cap - qfix;
     a.o_scr = ws.o_scr; a.m_scr = ws.m_scr; a.s_scr = ws.s_scr;
-    a.st = TileStatus{ws.st_word, ws.st_agg2, ws.st_inc2};
     a.tile_ctr = &ws.counters[0];
     a.err = ws.err;
     a.tot = ws.totals;
-    const int per_sm = 4;
-    size_t g = (size_t)sm_count() * per_sm;
-    int grid = (int)(ntiles < g ? ntiles : g);
+    // lanes per block: values per lane are 16 (float) / 8 (double)
+    const int per = dtype == 0 ? 16 : 8;
+    const int need = (bs + per - 1) / per;
+    const int G = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
     if (dtype == 0) {
-        if (E == 1) e = run_encode<float, 1, 4>(a, grid, s);
-        else if (E == 2) e = run_encode<float, 2, 4>(a, grid, s);
-        else if (E == 4) e = run_encode<float, 4, 4>(a, grid, s);
-        else e = run_encode<float, 8, 2>(a, grid, s);
+        switch (G) {
+            case 1: e = run_encode<float, 1>(a, s); break;
+            case 2: e = run_encode<float, 2>(a, s); break;
+            case 4: e = run_encode<float, 4>(a, s); break;
+            case 8: e = run_encode<float, 8>(a, s); break;
+            default: e = run_encode<float, 16>(a, s); break;
+        }
     } else {
-        if (E == 1) e = run_encode<double, 1, 4>(a, grid, s);
-        else if (E == 2) e = run_encode<double, 2, 4>(a, grid, s);
-        else if (E == 4) e = run_encode<double, 4, 4>(a, grid, s);
-        else e = run_encode<double, 8, 2>(a, grid, s);
+        switch (G) {
+            case 1: e = run_encode<double, 1>(a, s); break;
+            case 2: e = run_encode<double, 2>(a, s); break;
+            case 4: e = run_encode<double, 4>(a, s); break;
+            case 8: e = run_encode<double, 8>(a, s); break;
+            case 16: e = run_encode<double, 16>(a, s); break;
+            default: e = run_encode<double, 32>(a, s); break;
+        }
     }
     if (e != cudaSuccess) return e;
     int ag = (int)((nb + 255) / 256);
@@ -719,7 +811,10 @@ __global__ void __launch_bounds__(kIdxThreads) k_blocked_index(const uint8_t* s,
             unsigned long long k = first + i;
             if (famA) {
                 if (k < h.nnc) P[k] = run;
-                if (k == h.nnc - 1 && h.q_off + run + vals[i] > len) atomicExch(err, kErrStream);
+                if (k == h.nnc - 1) {
+                    P[h.nnc] = run + vals[i];
+                    if (h.q_off + run + vals[i] > len) atomicExch(err, kErrStream);
+                }
             } else if (k < nw) {
                 RW[k] = (uint32_t)run;
             }
@@ -729,38 +824,25 @@ __global__ void __launch_bounds__(kIdxThreads) k_blocked_index(const uint8_t* s,
     }
 }
 
-// Stage `n` stream bytes starting at src into shared memory at offset src % 16.
-__device__ __forceinline__ void warp_copy_in(uint8_t* stage, const uint8_t* src, uint32_t n, const uint8_t* s0,
-                                             const uint8_t* s1) {
-    const uint32_t sh = (uint32_t)((uintptr_t)src & 15);
-    const uint8_t* gbase = src - sh;
-    const uint32_t end = sh + n;
-    const uint32_t nch = (end + 15) >> 4;
-    for (uint32_t c = lane_id(); c < nch; c += 32) {
-        const uint8_t* lo = gbase + (c << 4);
-        if (lo >= s0 && lo + 16 <= s1) {
-            *(uint4*)(stage + (c << 4)) = __ldg((const uint4*)lo);
-        } else {
-            for (int j = 0; j < 16; j++) {
-                const uint8_t* q = lo + j;
-                stage[(c << 4) + j] = (q >= s0 && q < s1) ? q[0] : 0;
-            }
-        }
-    }
-}
-
-// Decode one non-constant block held in shared memory at p.
+// Decode one non-constant block whose payload sits in shared memory at p
+// (any alignment; the 16-byte-aligned buffer around it has >= 16 readable
+// bytes of slack).  Carried bytes: a value inherits its top `lead` bytes from
+// its predecessor, so lane values are first rebuilt with a zero carry, the
+// lane's final top three bytes and the lanes it wrote are scanned across the
+// warp ("last writer wins"), and the real carry is OR-ed into the byte lanes
+// still inherited -- the top min(lead so far) bytes.
 template <typename T, int E>
 __device__ __forceinline__ void dec_block(const uint8_t* p, int len, T* outb) {
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
+    constexpr int TOPSH = 8 * (W - 3);
     const int lane = (int)lane_id();
     const int reqLength = p[0];
     const uint32_t mb = ((uint32_t)p[1] << 24) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 8) | p[4];
-    const float med_f = __uint_as_float(mb);
     int R, s;
     split_reqlen(reqLength, &R, &s);
+    const int low = 8 * (W - R);                 // bits below the required bytes
     const int Lb = (len + 3) / 4;
     int nv = len - lane * E;
     nv = nv < 0 ? 0 : (nv > E ? E : nv);
@@ -770,52 +852,46 @@ __device__ __forceinline__ void dec_block(const uint8_t* p, int len, T* outb) {
                                       (2 * lane + 1 < Lb ? (uint32_t)p[6 + 2 * lane] : 0u);
     else if constexpr (E == 2) codes = lane / 2 < Lb ? ((uint32_t)p[5 + lane / 2] >> ((lane & 1) ? 0 : 4)) & 0xF : 0;
     else codes = lane / 4 < Lb ? ((uint32_t)p[5 + lane / 4] >> (6 - 2 * (lane & 3))) & 3 : 0;
-    int cnt[E];
+    int ld[E], cnt[E];
     uint32_t lane_bytes = 0;
 #pragma unroll
     for (int e = 0; e < E; e++) {
-        int ld = (codes >> (2 * (E - 1 - e))) & 3;
-        int c = R - ld;
+        ld[e] = (codes >> (2 * (E - 1 - e))) & 3;
+        int c = R - ld[e];
         cnt[e] = (e < nv && c > 0) ? c : 0;
         lane_bytes += cnt[e];
     }
     const uint32_t incl = warp_inclusive_sum(lane_bytes);
-    uint32_t q = (uint32_t)((uintptr_t)p & 15) + 5 + Lb + (incl - lane_bytes);
-    const uint32_t* buf = (const uint32_t*)((uintptr_t)p & ~(uintptr_t)15);
-    // stored parts, placed at their byte lanes
-    U sp[E];
+    const uint32_t base = (uint32_t)((uintptr_t)p & 15);
+    const uint32_t* buf = (const uint32_t*)((uintptr_t)p - base);
+    uint32_t q = base + 5 + Lb + (incl - lane_bytes);
+    // stored bytes in place, then the zero-carry reconstruction
+    U cur[E];
+    U run = 0;
+    int mld = 3;
 #pragma unroll
     for (int e = 0; e < E; e++) {
-        uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
-        uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
+        const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
+        const uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
+        U sp;
         if constexpr (sizeof(T) == 4) {
-            uint32_t m = cnt[e] >= 4 ? 0xFFFFFFFFu : ((1u << (8 * cnt[e])) - 1);
-            sp[e] = (lo & m) << (8 * (W - R));
+            sp = (lo & __funnelshift_rc(0xFFFFFFFFu, 0u, 32 - 8 * cnt[e])) << low;   // clamped: cnt 0 -> mask 0
         } else {
-            uint32_t w2 = buf[(q >> 2) + 2];
-            uint32_t hi = __funnelshift_r(w1, w2, (q & 3) * 8);
-            unsigned long long v = ((unsigned long long)hi << 32) | lo;
-            unsigned long long m = cnt[e] >= 8 ? ~0ull : ((1ull << (8 * cnt[e])) - 1);
-            sp[e] = (v & m) << (8 * (W - R));
+            const uint32_t w2 = buf[(q >> 2) + 2];
+            const uint32_t hi = __funnelshift_r(w1, w2, (q & 3) * 8);
+            const unsigned long long v = ((unsigned long long)hi << 32) | lo;
+            const unsigned long long m = cnt[e] >= 8 ? ~0ull : ((1ull << (8 * cnt[e])) - 1);
+            sp = (v & m) << low;
         }
         q += cnt[e];
+        const U inh = ~(~(U)0 >> (8 * ld[e]));   // the top ld[e] bytes come from the predecessor
+        run = sp | (run & inh);
+        cur[e] = run;
+        if (e < nv) mld = ld[e] < mld ? ld[e] : mld;
     }
-    // top three byte lanes: the only ones a value can inherit from its
-    // predecessor.  Packed summary: bits 0..23 bytes W-3..W-1, bits 24..26 written.
-    constexpr int TOPSH = 8 * (W - 3);
-    uint32_t sv = 0, sm = 0;
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-        if (e < nv) {
-            int ld = (codes >> (2 * (E - 1 - e))) & 3;
-            uint32_t wm = (1u << (3 - ld)) - 1;                       // lanes written: W-3 .. W-1-ld
-            uint32_t wb = (wm & 1) * 0xFFu | (wm & 2) * 0x7F80u | (wm & 4) * 0x3FC000u;
-            uint32_t top = (uint32_t)(sp[e] >> TOPSH) & 0xFFFFFFu;
-            sv = (sv & ~wb) | (top & wb);
-            sm |= wm;
-        }
-    }
-    uint32_t sum = (sm << 24) | sv;
+    // lane summary: top three bytes of its last value, and which of them it wrote
+    const uint32_t wm = nv ? (1u << (3 - mld)) - 1 : 0u;
+    uint32_t sum = (wm << 24) | ((uint32_t)(run >> TOPSH) & 0xFFFFFFu);
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
         uint32_t o = __shfl_up_sync(0xffffffffu, sum, d);
@@ -826,98 +902,164 @@ __device__ __forceinline__ void dec_block(const uint8_t* p, int len, T* outb) {
         }
     }
     uint32_t ex = __shfl_up_sync(0xffffffffu, sum, 1);
-    if (lane == 0) ex = 0;   // previous value at block start is zero
-    U prev = (U)(ex & 0xFFFFFFu) << TOPSH;
-    const T med = widen_median<T>(med_f);
+    if (lane == 0) ex = 0;   // the value before a block is zero
+    const U carry = (U)(ex & 0xFFFFFFu) << TOPSH;
+    const T med = widen_median<T>(__uint_as_float(mb));
     T v[E];
     bool bad = false;
+    int cm = 3;
 #pragma unroll
     for (int e = 0; e < E; e++) {
-        int ld = (codes >> (2 * (E - 1 - e))) & 3;
-        U inh = ld ? ~(((U)1 << (8 * (W - ld))) - 1) : (U)0;       // top `ld` bytes come from prev
-        U cur = sp[e] | (prev & inh);
-        sp[e] = cur << s;
-        v[e] = EL::add(EL::of(sp[e]), med);
+        cm = ld[e] < cm ? ld[e] : cm;
+        const U keep = ~(~(U)0 >> (8 * cm));       // byte lanes still inherited from before this lane
+        cur[e] = (cur[e] | (carry & keep)) << s;
+        v[e] = EL::add(EL::of(cur[e]), med);
         bad |= v[e] != v[e];
-        prev = cur;
     }
     if (__any_sync(0xffffffffu, bad)) {
 #pragma unroll
-        for (int e = 0; e < E; e++) v[e] = xadd(EL::of(sp[e]), med);
+        for (int e = 0; e < E; e++) v[e] = xadd(EL::of(cur[e]), med);
     }
     store_lane<T, E>(outb + lane * E, nv, lane_vec_ok<T, E>(outb), v);
 }
 
 template <typename T, int E>
-constexpr int dec_stage_bytes() {
-    return ((16 + 5 + (32 * E + 3) / 4 + (int)sizeof(T) * 32 * E + 32 + 15) / 16) * 16;
-}
+struct DecTile {
+    static constexpr int kMaxPay = 5 + (32 * E + 3) / 4 + (int)sizeof(T) * 32 * E;
+    static constexpr int kBudget = 36 * 1024;
+    static constexpr int kBlocks = (kBudget / kMaxPay) >= 64 ? 64 : (kBudget / kMaxPay) >= 32 ? 32 : 16;
+    static constexpr int kStage = kBlocks * kMaxPay + 64;
+};
 
+// One CTA per tile of kBlocks blocks: the tile's state bits and non-constant
+// rank come from the index scans, its payloads are one contiguous byte range
+// copied into shared memory with aligned 16-byte loads, and each warp then
+// decodes its blocks out of shared memory.
 template <typename T, int E>
 __global__ void __launch_bounds__(kDecThreads) k_blocked_decode(const uint8_t* __restrict__ s, unsigned long long len,
                                                                 const BlockedHdr* hp,
                                                                 const unsigned long long* __restrict__ P,
                                                                 const uint32_t* __restrict__ RW, T* out,
                                                                 int native_medians, int* err) {
-    constexpr int STAGE = dec_stage_bytes<T, E>();
-    __shared__ __align__(16) uint8_t s_stage[kDecThreads / 32][STAGE];
+    using TL = DecTile<T, E>;
+    constexpr int TBD = TL::kBlocks;
+    __shared__ __align__(16) uint8_t stage[TL::kStage];
+    __shared__ unsigned long long s_p[TBD + 1];
+    __shared__ uint32_t s_rank[TBD];
+    __shared__ uint8_t s_nc[TBD];
+    __shared__ unsigned long long s_rank0, s_pa;
+    __shared__ uint32_t s_nnc;
+    __shared__ int s_bad;
     const BlockedHdr h = *hp;
     if (!h.ok) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned long long gw = (unsigned long long)blockIdx.x * (kDecThreads / 32) + warp;
-    const unsigned long long nwarps = (unsigned long long)gridDim.x * (kDecThreads / 32);
+    const unsigned long long ntiles = (h.nb + TBD - 1) / TBD;
     const uint8_t* send = s + len;
-    for (unsigned long long b = gw; b < h.nb; b += nwarps) {
-        const unsigned long long off = b * h.bs;
-        const unsigned long long rem = h.n - off;
-        const int blen = rem < h.bs ? (int)rem : (int)h.bs;
-        // state bit and non-constant rank
-        const unsigned long long w = b >> 5;
-        uint32_t word = 0;
+    for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const unsigned long long b0 = tile * TBD;
+        // state bits and ranks within the tile (TBD <= 64: two warps)
+        if (threadIdx.x < 64) {   // whole warps 0 and 1
+            const bool in = threadIdx.x < TBD;
+            const unsigned long long b = b0 + threadIdx.x;
+            const uint32_t bit = (in && b < h.nb) ? (s[h.s_off + (b >> 3)] >> (7 - (b & 7))) & 1u : 0u;
+            const unsigned m = __ballot_sync(0xffffffffu, bit);
+            if (in) {
+                s_nc[threadIdx.x] = (uint8_t)bit;
+                s_rank[threadIdx.x] = __popc(m & ((1u << lane) - 1));   // rank within its warp; fixed below
+            }
+            if (lane == 31) s_p[warp] = __popc(m);                     // warp totals (scratch use of s_p)
+        }
+        if (threadIdx.x == 0) {
+            const unsigned long long w = b0 >> 5;
+            uint32_t word = 0;
+            for (int j = 0; j < 4; j++) {
+                unsigned long long bi = 4 * w + j;
+                word = (word << 8) | (bi < h.sb ? (uint32_t)s[h.s_off + bi] : 0u);
+            }
+            const int bit = (int)(b0 & 31);
+            s_rank0 = RW[w] + (bit ? __popc(word >> (32 - bit)) : 0);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t tot = (uint32_t)s_p[0] + (TBD > 32 ? (uint32_t)s_p[1] : 0u);
+            s_nnc = tot;
+        }
+        if (TBD > 32 && threadIdx.x >= 32 && threadIdx.x < TBD) s_rank[threadIdx.x] += (uint32_t)s_p[0];
+        __syncthreads();
+        const uint32_t nnc_t = s_nnc;
+        const unsigned long long r0 = s_rank0;
+        if (threadIdx.x <= nnc_t && nnc_t > 0) s_p[threadIdx.x] = P[r0 + threadIdx.x];
+        if (threadIdx.x == 0) s_bad = 0;
+        __syncthreads();
+        if (nnc_t > 0) {
+            const unsigned long long pa = s_p[0], pb = s_p[nnc_t];
+            if (threadIdx.x == 0) {
+                s_pa = pa;
+                if (pb < pa || pb - pa + 32 > (unsigned long long)TL::kStage || h.q_off + pb > len) {
+                    s_bad = 1;
+                    atomicExch(err, kErrStream);
+                }
+            }
+            __syncthreads();
+            if (!s_bad) {
+                // the tile's payloads: one contiguous range, staged at its own 16-byte phase
+                const uint8_t* src = s + h.q_off + pa;
+                const uint32_t sh = (uint32_t)((uintptr_t)src & 15);
+                const uint8_t* gbase = src - sh;
+                const uint32_t nch = (uint32_t)((sh + (pb - pa) + 15) >> 4);
+                for (uint32_t c = threadIdx.x; c < nch; c += kDecThreads) {
+                    const uint8_t* lo = gbase + (c << 4);
+                    if (lo >= s && lo + 16 <= send) *(uint4*)(stage + (c << 4)) = __ldg((const uint4*)lo);
+                    else
+                        for (int j = 0; j < 16; j++) stage[(c << 4) + j] = (lo + j >= s && lo + j < send) ? lo[j] : 0;
+                }
+            }
+        }
+        __syncthreads();
+        const bool bad = nnc_t > 0 && s_bad;
+        for (int k = warp; k < TBD; k += kDecThreads / 32) {
+            const unsigned long long b = b0 + k;
+            if (b >= h.nb) break;
+            const unsigned long long off = b * h.bs;
+            const unsigned long long rem = h.n - off;
+            const int blen = rem < h.bs ? (int)rem : (int)h.bs;
+            T* ob = out + off;
+            if (!s_nc[k]) {
+                const unsigned long long rank = r0 + s_rank[k];
+                const uint8_t* mp = s + h.m_off + 4 * (b - rank);
+                uint32_t mbits = native_medians
+                                     ? ((uint32_t)mp[0] | ((uint32_t)mp[1] << 8) | ((uint32_t)mp[2] << 16) | ((uint32_t)mp[3] << 24))
+                                     : (((uint32_t)mp[0] << 24) | ((uint32_t)mp[1] << 16) | ((uint32_t)mp[2] << 8) | mp[3]);
+                const T m = widen_median<T>(__uint_as_float(mbits));
+                int nv = blen - lane * E;
+                nv = nv < 0 ? 0 : (nv > E ? E : nv);
+                T v[E];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            unsigned long long bi = 4 * w + j;
-            word = (word << 8) | (bi < h.sb ? (uint32_t)s[h.s_off + bi] : 0u);
+                for (int e = 0; e < E; e++) v[e] = m;
+                store_lane<T, E>(ob + lane * E, nv, lane_vec_ok<T, E>(ob), v);
+                continue;
+            }
+            if (bad) continue;
+            const uint32_t r = s_rank[k];
+            const unsigned long long pofs = s_p[r] - s_pa, size = s_p[r + 1] - s_p[r];
+            const uint32_t minsz = 5 + (uint32_t)((blen + 3) / 4);
+            if (size < minsz || size > (unsigned long long)TL::kMaxPay) {
+                if (lane == 0) atomicExch(err, kErrStream);
+                continue;
+            }
+            const uint32_t sh = (uint32_t)((uintptr_t)(s + h.q_off + s_pa) & 15);
+            dec_block<T, E>(stage + sh + pofs, blen, ob);
         }
-        const int bit = (int)(b & 31);
-        const bool nonconst = (word >> (31 - bit)) & 1;
-        const unsigned long long rank = RW[w] + (bit ? __popc(word >> (32 - bit)) : 0);
-        T* ob = out + off;
-        if (!nonconst) {
-            const uint8_t* mp = s + h.m_off + 4 * (b - rank);
-            uint32_t mbits = native_medians
-                                 ? ((uint32_t)mp[0] | ((uint32_t)mp[1] << 8) | ((uint32_t)mp[2] << 16) | ((uint32_t)mp[3] << 24))
-                                 : (((uint32_t)mp[0] << 24) | ((uint32_t)mp[1] << 16) | ((uint32_t)mp[2] << 8) | mp[3]);
-            T m = widen_median<T>(__uint_as_float(mbits));
-            int nv = blen - lane * E;
-            nv = nv < 0 ? 0 : (nv > E ? E : nv);
-            T v[E];
-#pragma unroll
-            for (int e = 0; e < E; e++) v[e] = m;
-            store_lane<T, E>(ob + lane * E, nv, lane_vec_ok<T, E>(ob), v);
-            continue;
-        }
-        const unsigned long long po = h.q_off + P[rank];
-        const uint32_t size = (uint32_t)s[h.o_off + 2 * rank] | ((uint32_t)s[h.o_off + 2 * rank + 1] << 8);
-        const uint32_t minsz = 5 + (uint32_t)((blen + 3) / 4);
-        if (po + size > len || size < minsz || size + 32 > (uint32_t)STAGE) {
-            if (lane == 0) atomicExch(err, kErrStream);
-            continue;
-        }
-        uint8_t* st = s_stage[warp];
-        warp_copy_in(st, s + po, size, s, send);
-        __syncwarp();
-        dec_block<T, E>(st + ((uintptr_t)(s + po) & 15), blen, ob);
-        __syncwarp();
+        __syncthreads();
     }
 }
 
 template <typename T, int E>
 static void run_decode(const uint8_t* s, size_t len, size_t nb, const Workspace& ws, void* out, int native,
                        cudaStream_t st) {
-    size_t want = (nb + (kDecThreads / 32) - 1) / (kDecThreads / 32);
-    size_t cap = (size_t)sm_count() * 8;
-    int grid = (int)(want < cap ? (want ? want : 1) : cap);
+    const size_t tiles = (nb + DecTile<T, E>::kBlocks - 1) / DecTile<T, E>::kBlocks;
+    const size_t cap = (size_t)sm_count() * 4;
+    int grid = (int)(tiles < cap ? (tiles ? tiles : 1) : cap);
     TraceScope tr("blocked_decode", st);
     k_blocked_decode<T, E><<<grid, kDecThreads, 0, st>>>(s, len, ws.bhdr, ws.p_off, ws.rank_w, (T*)out, native,
                                                          ws.err);

@@ -265,4 +265,339 @@ __device__ __forceinline__ void lookback(TileStatus st, long long tile, unsigned
     *ex_b = pb;
 }
 
+// ------------------------------------------------------------------ TMA bulk copies + mbarriers
+//
+// One thread arms an mbarrier with the byte count and issues a 1-D bulk copy
+// (cp.async.bulk) global -> shared; consumers wait on the barrier's phase.
+// Source, destination and size must be multiples of 16 bytes.
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up (returns false) after kSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+    for (unsigned i = 0; i < (1u << 22); i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (i > 16) __nanosleep(64);
+    }
+    return false;
+}
+
+// ------------------------------------------------------------------ wide look-back
+//
+// Tile status as one 32-bit word: [31:30] flag (0 empty, 1 aggregate,
+// 2 inclusive), [29:23] the tile's second count (<= 127), [22:0] the tile's
+// byte count (< 8 MiB).  Inclusive prefixes (64-bit) live in side arrays
+// written before the inclusive flag is released.  A walking warp reads 8
+// consecutive status words per lane (two 16-byte loads), i.e. 256
+// predecessors per memory round trip: the rate at which tiles can be placed
+// is then (256 / round-trip latency) instead of 32 / latency, which is what
+// lets a look-back over 16-32 KiB tiles keep up with HBM3e.
+struct TileStatus32 {
+    uint32_t* st;                  // [ntiles + 8], zeroed before the launch
+    unsigned long long* inc_a;     // [ntiles]
+    unsigned long long* inc_b;     // [ntiles]
+};
+constexpr uint32_t kSt32Agg = 1u << 30, kSt32Inc = 2u << 30;
+
+__device__ __forceinline__ void st_volatile32(uint32_t* p, uint32_t v) {
+    asm volatile("st.volatile.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint4 ld_volatile_v4(const uint32_t* p) {
+    uint4 v;
+    asm volatile("ld.volatile.global.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p)
+                 : "memory");
+    return v;
+}
+
+// Second-value policies of the wide look-back.
+// SumPolicy: the 7-bit field is a count, prefixes add.
+struct SumPolicy {
+    static __device__ __forceinline__ unsigned long long contrib(uint32_t f, long long) { return f; }
+    static __device__ __forceinline__ unsigned long long op(unsigned long long x, unsigned long long y) { return x + y; }
+    static __device__ __forceinline__ unsigned long long reduce(unsigned long long v) { return warp_sum(v); }
+};
+// WriterPolicy: the field's three bits say which of the top three byte lanes
+// the tile stored; the prefix is, per lane, the latest such tile (+1, 21 bits
+// each, 0 = none), combined by max.
+struct WriterPolicy {
+    static __device__ __forceinline__ unsigned long long contrib(uint32_t f, long long u) {
+        unsigned long long t = (unsigned long long)(u + 1);
+        return ((f & 1) ? t : 0ull) | ((f & 2) ? t << 21 : 0ull) | ((f & 4) ? t << 42 : 0ull);
+    }
+    static __device__ __forceinline__ unsigned long long op(unsigned long long x, unsigned long long y) {
+        return Max3x21Op::op(x, y);
+    }
+    static __device__ __forceinline__ unsigned long long reduce(unsigned long long v) {
+        return Max3x21Op::warp_reduce(v);
+    }
+};
+
+// Whole warp.  agg_a < 2^23 (a sum), agg_b < 128 (combined by Policy).
+// Returns the exclusive prefixes.
+template <typename Policy = SumPolicy>
+__device__ __forceinline__ void lookback_wide(TileStatus32 s, long long tile, uint32_t agg_a, uint32_t agg_b,
+                                              unsigned long long* ex_a, unsigned long long* ex_b, int* err) {
+    const unsigned lane = lane_id();
+    const uint32_t packed = (agg_b << 23) | (agg_a & 0x7FFFFFu);
+    const unsigned long long self_b = Policy::contrib(agg_b, tile);
+    if (tile == 0) {
+        if (lane == 0) {
+            __stcg(&s.inc_a[0], (unsigned long long)agg_a);
+            __stcg(&s.inc_b[0], self_b);
+            __threadfence();
+            st_volatile32(&s.st[0], kSt32Inc | packed);
+        }
+        *ex_a = 0;
+        *ex_b = 0;
+        return;
+    }
+    if (lane == 0) st_volatile32(&s.st[tile], kSt32Agg | packed);
+    unsigned long long pa = 0, pb = 0;
+    long long g0 = ((tile - 1) >> 3) << 3;   // group of 8 holding the nearest predecessor
+    unsigned spins = 0;
+    bool failed = false;
+    while (true) {
+        const long long g = g0 - 8 * (long long)lane;
+        uint32_t w[8];
+        if (g >= 0) {
+            uint4 a = ld_volatile_v4(s.st + g), b = ld_volatile_v4(s.st + g + 4);
+            w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w; w[4] = b.x; w[5] = b.y; w[6] = b.z; w[7] = b.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; j++) w[j] = kSt32Inc;   // before tile 0: an inclusive zero
+        }
+        // nearest inclusive predecessor in this lane (highest index), and the
+        // readiness / combination of the aggregates above it
+        int inc_j = -1;
+        bool ready = true;
+        uint32_t sa = 0;
+        unsigned long long sb = 0;
+#pragma unroll
+        for (int j = 7; j >= 0; j--) {
+            const long long u = g + j;
+            const bool pred = u < tile;
+            const uint32_t f = w[j] & 0xC0000000u;
+            if (pred && inc_j < 0) {
+                if (f == kSt32Inc) inc_j = j;
+                else {
+                    ready = ready && f != 0;
+                    sa += w[j] & 0x7FFFFFu;
+                    sb = Policy::op(sb, Policy::contrib((w[j] >> 23) & 0x7Fu, u));
+                }
+            }
+        }
+        const unsigned inc_mask = __ballot_sync(0xffffffffu, inc_j >= 0);
+        const unsigned stop = inc_mask ? (unsigned)__ffs(inc_mask) - 1 : 31u;
+        const unsigned window = stop == 31u ? 0xffffffffu : ((1u << (stop + 1)) - 1);
+        if (__ballot_sync(0xffffffffu, !ready) & window) {
+            if (++spins > kSpinLimit) { failed = true; break; }
+            __nanosleep(spins < 64 ? 32 : 256);
+            continue;
+        }
+        unsigned long long va = 0, vb = 0;
+        if (lane <= stop) { va = sa; vb = sb; }
+        if (lane == stop && inc_j >= 0 && g + inc_j >= 0) {
+            __threadfence();
+            va += __ldcg(&s.inc_a[g + inc_j]);
+            vb = Policy::op(vb, __ldcg(&s.inc_b[g + inc_j]));
+        }
+        pa += warp_sum(va);
+        pb = Policy::op(pb, Policy::reduce(vb));
+        if (inc_mask) break;
+        g0 -= 256;
+    }
+    if (failed && lane == 0) atomicExch(err, kErrLookback);
+    if (lane == 0) {
+        __stcg(&s.inc_a[tile], pa + agg_a);
+        __stcg(&s.inc_b[tile], Policy::op(pb, self_b));
+        __threadfence();
+        st_volatile32(&s.st[tile], kSt32Inc | packed);
+    }
+    *ex_a = pa;
+    *ex_b = pb;
+}
+
+// The wide look-back in two halves, so a tile's aggregate can be published
+// well before its prefix is needed (software-pipelined placement).
+template <typename Policy = SumPolicy>
+__device__ __forceinline__ void lookback_publish(TileStatus32 s, long long tile, uint32_t agg_a, uint32_t agg_b) {
+    if (lane_id() != 0) return;
+    const uint32_t packed = (agg_b << 23) | (agg_a & 0x7FFFFFu);
+    if (tile == 0) {
+        __stcg(&s.inc_a[0], (unsigned long long)agg_a);
+        __stcg(&s.inc_b[0], Policy::contrib(agg_b, 0));
+        __threadfence();
+        st_volatile32(&s.st[0], kSt32Inc | packed);
+    } else {
+        st_volatile32(&s.st[tile], kSt32Agg | packed);
+    }
+}
+
+// Whole warp; the tile's aggregate must already be published.
+template <typename Policy = SumPolicy>
+__device__ __forceinline__ void lookback_resolve(TileStatus32 s, long long tile, uint32_t agg_a, uint32_t agg_b,
+                                                 unsigned long long* ex_a, unsigned long long* ex_b, int* err) {
+    const unsigned lane = lane_id();
+    if (tile == 0) {
+        *ex_a = 0;
+        *ex_b = 0;
+        return;
+    }
+    const uint32_t packed = (agg_b << 23) | (agg_a & 0x7FFFFFu);
+    const unsigned long long self_b = Policy::contrib(agg_b, tile);
+    unsigned long long pa = 0, pb = 0;
+    long long g0 = ((tile - 1) >> 3) << 3;
+    unsigned spins = 0;
+    bool failed = false;
+    while (true) {
+        const long long g = g0 - 8 * (long long)lane;
+        uint32_t w[8];
+        if (g >= 0) {
+            uint4 a = ld_volatile_v4(s.st + g), b = ld_volatile_v4(s.st + g + 4);
+            w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w; w[4] = b.x; w[5] = b.y; w[6] = b.z; w[7] = b.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; j++) w[j] = kSt32Inc;
+        }
+        int inc_j = -1;
+        bool ready = true;
+        uint32_t sa = 0;
+        unsigned long long sb = 0;
+#pragma unroll
+        for (int j = 7; j >= 0; j--) {
+            const long long u = g + j;
+            const bool pred = u < tile;
+            const uint32_t f = w[j] & 0xC0000000u;
+            if (pred && inc_j < 0) {
+                if (f == kSt32Inc) inc_j = j;
+                else {
+                    ready = ready && f != 0;
+                    sa += w[j] & 0x7FFFFFu;
+                    sb = Policy::op(sb, Policy::contrib((w[j] >> 23) & 0x7Fu, u));
+                }
+            }
+        }
+        const unsigned inc_mask = __ballot_sync(0xffffffffu, inc_j >= 0);
+        const unsigned stop = inc_mask ? (unsigned)__ffs(inc_mask) - 1 : 31u;
+        const unsigned window = stop == 31u ? 0xffffffffu : ((1u << (stop + 1)) - 1);
+        if (__ballot_sync(0xffffffffu, !ready) & window) {
+            if (++spins > kSpinLimit) { failed = true; break; }
+            __nanosleep(spins < 64 ? 32 : 256);
+            continue;
+        }
+        unsigned long long va = 0, vb = 0;
+        if (lane <= stop) { va = sa; vb = sb; }
+        if (lane == stop && inc_j >= 0 && g + inc_j >= 0) {
+            __threadfence();
+            va += __ldcg(&s.inc_a[g + inc_j]);
+            vb = Policy::op(vb, __ldcg(&s.inc_b[g + inc_j]));
+        }
+        pa += warp_sum(va);
+        pb = Policy::op(pb, Policy::reduce(vb));
+        if (inc_mask) break;
+        g0 -= 256;
+    }
+    if (failed && lane == 0) atomicExch(err, kErrLookback);
+    if (lane == 0) {
+        __stcg(&s.inc_a[tile], pa + agg_a);
+        __stcg(&s.inc_b[tile], Policy::op(pb, self_b));
+        __threadfence();
+        st_volatile32(&s.st[tile], kSt32Inc | packed);
+    }
+    *ex_a = pa;
+    *ex_b = pb;
+}
+
+// ------------------------------------------------------------------ inline-prefix look-back
+//
+// One 64-bit status word per tile: [63:62] flag (0 empty, 1 aggregate,
+// 2 inclusive), [61:0] the tile's byte count (aggregate) or the inclusive
+// prefix itself.  Resolving a tile is then one memory round trip per window
+// of 128 predecessors (4 words per lane), with no second load for the prefix.
+constexpr unsigned long long kS64Agg = 1ull << 62, kS64Inc = 2ull << 62, kS64Val = (1ull << 62) - 1;
+
+__device__ __forceinline__ void st_volatile64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.volatile.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void ld_volatile_v2x2(const unsigned long long* p, unsigned long long (&w)[4]) {
+    unsigned long long a, b, c, d;
+    asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+    asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(c), "=l"(d) : "l"(p + 2) : "memory");
+    w[0] = a; w[1] = b; w[2] = c; w[3] = d;
+}
+
+// Lane 0 publishes the tile's aggregate (tile 0 publishes its inclusive value).
+__device__ __forceinline__ void prefix_publish(unsigned long long* st, long long tile, unsigned long long agg) {
+    if (lane_id() != 0) return;
+    st_volatile64(&st[tile], (tile == 0 ? kS64Inc : kS64Agg) | (agg & kS64Val));
+}
+
+// Whole warp: exclusive prefix of `tile` (aggregate already published), then
+// publish its inclusive value.  `st` holds ntiles + 4 zeroed words.
+__device__ __forceinline__ unsigned long long prefix_resolve(unsigned long long* st, long long tile,
+                                                            unsigned long long agg, int* err) {
+    if (tile == 0) return 0;
+    const unsigned lane = lane_id();
+    unsigned long long pa = 0;
+    long long g0 = ((tile - 1) >> 2) << 2;
+    unsigned spins = 0;
+    bool failed = false;
+    while (true) {
+        const long long g = g0 - 4 * (long long)lane;
+        unsigned long long w[4];
+        if (g >= 0) ld_volatile_v2x2(st + g, w);
+        else { w[0] = w[1] = w[2] = w[3] = kS64Inc; }
+        int inc_j = -1;
+        bool ready = true;
+        unsigned long long sa = 0;
+#pragma unroll
+        for (int j = 3; j >= 0; j--) {
+            const unsigned long long f = w[j] & ~kS64Val;
+            if (g + j < tile && inc_j < 0) {
+                if (f == kS64Inc) { inc_j = j; sa += w[j] & kS64Val; }
+                else { ready = ready && f != 0; sa += w[j] & kS64Val; }
+            }
+        }
+        const unsigned inc_mask = __ballot_sync(0xffffffffu, inc_j >= 0);
+        const unsigned stop = inc_mask ? (unsigned)__ffs(inc_mask) - 1 : 31u;
+        const unsigned window = stop == 31u ? 0xffffffffu : ((1u << (stop + 1)) - 1);
+        if (__ballot_sync(0xffffffffu, !ready) & window) {
+            if (++spins > kSpinLimit) { failed = true; break; }
+            __nanosleep(spins < 64 ? 32 : 256);
+            continue;
+        }
+        pa += warp_sum(lane <= stop ? sa : 0ull);
+        if (inc_mask) break;
+        g0 -= 128;
+    }
+    if (failed && lane == 0) atomicExch(err, kErrLookback);
+    if (lane == 0) st_volatile64(&st[tile], kS64Inc | ((pa + agg) & kS64Val));
+    return pa;
+}
+
 }  // namespace szxg

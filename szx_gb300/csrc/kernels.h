@@ -65,6 +65,7 @@ struct Workspace {
     NonBlockedHdr* nhdr;
     int* err;
     unsigned long long* counters;   // 4 tile counters
+    uint32_t* st32;                 // 32-bit tile status words ([status_tiles + 16])
     unsigned long long* st_word;    // tile status words (family A)
     unsigned long long* st_agg2;
     unsigned long long* st_inc2;

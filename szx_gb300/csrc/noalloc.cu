@@ -9,7 +9,7 @@
 // g_noalloc_scratch below.
 //
 // Cost and limits:
-// * every GPU that loads this library holds kNoAllocBytes (about 7.7 MiB) of
+// * every GPU that loads this library holds kNoAllocBytes (about 8.0 MiB) of
 //   device memory for the array until the process exits;
 // * one call handles at most kNoAllocMaxBlocks = 1,048,576 blocks
 //   (ceil(nbEle / blockSize)), i.e. 134,217,728 values at blockSize 128;
@@ -35,7 +35,8 @@ constexpr size_t kNoAllocMaxBlocks = size_t(1) << 20;
 constexpr size_t kNoAllocHeader = 4096;
 constexpr size_t kNoAllocTiles = kNoAllocMaxBlocks / 16 + 2;   // tiles of >= 16 blocks
 constexpr size_t na_a256(size_t x) { return (x + 255) & ~size_t(255); }
-constexpr size_t kNaSt = kNoAllocHeader;
+constexpr size_t kNaSt32 = kNoAllocHeader;
+constexpr size_t kNaSt = kNaSt32 + na_a256(4 * (kNoAllocTiles + 16));
 constexpr size_t kNaPartials = kNaSt + na_a256(3 * 8 * kNoAllocTiles);
 constexpr size_t kNaO = kNaPartials + na_a256(4096 * 24);
 constexpr size_t kNaM = kNaO + na_a256(2 * kNoAllocMaxBlocks);
@@ -76,6 +77,7 @@ Workspace carve(unsigned char* b) {
     w.result = (StreamResult*)(h + 128);
     w.err = (int*)(h + 448);
     w.counters = (unsigned long long*)(h + 512);
+    w.st32 = (uint32_t*)(b + kNaSt32);
     w.st_word = (unsigned long long*)(b + kNaSt);
     w.st_agg2 = w.st_word + kNoAllocTiles;
     w.st_inc2 = w.st_agg2 + kNoAllocTiles;

@@ -50,12 +50,16 @@ __device__ __forceinline__ void cta_copy_out(const uint8_t* stage, uint32_t sh, 
     uint8_t* gbase = dst - sh;
     const uint32_t end = sh + n, nch = (end + 15) >> 4;
     for (uint32_t c = threadIdx.x; c < nch; c += blockDim.x) {
-        uint32_t lo = c << 4, hi = lo + 16;
-        if (lo >= sh && hi <= end) *(uint4*)(gbase + lo) = *(const uint4*)(stage + lo);
-        else {
-            uint32_t a = lo > sh ? lo : sh, b = hi < end ? hi : end;
-            for (uint32_t j = a; j < b; j++) gbase[j] = stage[j];
-        }
+        uint32_t lo = c << 4;
+        if (lo >= sh && lo + 16 <= end) *(uint4*)(gbase + lo) = *(const uint4*)(stage + lo);
+    }
+    // partial head chunk: threads 0-15, partial tail chunk: threads 16-31
+    if (threadIdx.x < 32) {
+        const uint32_t last = nch - 1;
+        const uint32_t c = threadIdx.x < 16 ? 0 : last;
+        const bool part = threadIdx.x < 16 ? (sh > 0 || end < 16) : (last > 0 && (end & 15) != 0);
+        const uint32_t b = (c << 4) + (threadIdx.x & 15);
+        if (part && b >= sh && b < end) gbase[b] = stage[b];
     }
 }
 
@@ -128,7 +132,7 @@ struct NbEncArgs {
     unsigned long long n, ntiles, cap;
     const CodecParams* params;
     uint8_t* out;
-    TileStatus st;
+    TileStatus32 st;
     unsigned long long* tile_ctr;
     int* err;
     StreamResult* res;
@@ -211,7 +215,7 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
         const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);
         if (threadIdx.x < 32) {
             unsigned long long base, dummy;
-            lookback(a.st, tile, total, 0, &base, &dummy, a.err);
+            lookback_wide(a.st, tile, total, 0, &base, &dummy, a.err);
             if (threadIdx.x == 0) {
                 s_base = base;
                 const bool ok = base + total <= mid_cap;
@@ -278,12 +282,12 @@ cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t
     if (n == 0 || cap < nonblocked_bound(dtype, n) - 64) return cudaErrorInvalidValue;
     const size_t ntiles = (n + kNbTile - 1) / kNbTile;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(ws.st_word, 0, sizeof(unsigned long long) * ntiles, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ws.st32, 0, sizeof(uint32_t) * (ntiles + 8), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ws.counters, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ws.err, 0, sizeof(int), s)) != cudaSuccess) return e;
     NbEncArgs a;
     a.x = x; a.n = n; a.ntiles = ntiles; a.cap = cap; a.params = ws.params; a.out = d_out;
-    a.st = TileStatus{ws.st_word, ws.st_agg2, ws.st_inc2};
+    a.st = TileStatus32{ws.st32, ws.st_agg2, ws.st_inc2};
     a.tile_ctr = &ws.counters[0];
     a.err = ws.err;
     a.res = ws.result;
@@ -334,7 +338,7 @@ __device__ __forceinline__ uint32_t lead_word(const uint8_t* lead, unsigned long
 // bits, tile+1), aux[3t+2] = own writer positions (3x21 bits, pos+1).
 template <typename T>
 __global__ void __launch_bounds__(kNbThreads) k_nb_summary(const uint8_t* s, const NonBlockedHdr* hp,
-                                                           unsigned long long* aux, TileStatus st,
+                                                           unsigned long long* aux, TileStatus32 st,
                                                            unsigned long long* ctr, int* err) {
     constexpr int W = Elem<T>::W;
     __shared__ uint32_t s_sum[8];
@@ -379,18 +383,19 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_summary(const uint8_t* s, con
             if (lane == 0) s_pos[k][warp] = p;
         }
         __syncthreads();
-        unsigned long long own = 0, latest = 0;
+        unsigned long long own = 0;
+        uint32_t wrote = 0;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             int p = -1;
             for (int w = 0; w < kNbThreads / 32; w++) p = max(p, s_pos[k][w]);
             gpos[k] = p;
             own |= (unsigned long long)(p + 1) << (21 * k);
-            if (p >= 0) latest |= (unsigned long long)(tile + 1) << (21 * k);
+            if (p >= 0) wrote |= 1u << k;
         }
         if (threadIdx.x < 32) {
             unsigned long long base, lw;
-            lookback<Max3x21Op>(st, tile, total, latest, &base, &lw, err);
+            lookback_wide<WriterPolicy>(st, tile, total, wrote, &base, &lw, err);
             if (threadIdx.x == 0) {
                 aux[3 * tile] = base;
                 aux[3 * tile + 1] = lw;
@@ -544,7 +549,7 @@ cudaError_t launch_nonblocked_decode(int dtype, const uint8_t* d_stream, size_t 
     const size_t ntiles = (n + kNbTile - 1) / kNbTile;
     if (ntiles >= (1u << 21) - 1) return cudaErrorInvalidValue;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(ws.st_word, 0, sizeof(unsigned long long) * ntiles, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ws.st32, 0, sizeof(uint32_t) * (ntiles + 8), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ws.counters, 0, 2 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
     {
         TraceScope tr("nonblocked_parse", s);
@@ -552,7 +557,7 @@ cudaError_t launch_nonblocked_decode(int dtype, const uint8_t* d_stream, size_t 
     }
     size_t g = (size_t)sm_count() * 8;
     int grid = (int)(ntiles < g ? ntiles : g);
-    TileStatus st{ws.st_word, ws.st_agg2, ws.st_inc2};
+    TileStatus32 st{ws.st32, ws.st_agg2, ws.st_inc2};
     {
         TraceScope tr("nonblocked_summary", s);
         if (dtype == 0)
