@@ -149,7 +149,7 @@ int SZxG_workspace_status(const void* d_workspace, void* stream);
 /* No counterpart in the reference.  SZxG_compress for the blocked layouts
  * (fastMode 2, 3, 4) that allocates nothing: its scratch is a fixed array in
  * device memory that every GPU loading this library holds until exit (about
- * 8.0 MiB).  For callers that may not call cudaMalloc -- applications whose
+ * 7.2 MiB).  For callers that may not call cudaMalloc -- applications whose
  * own pool allocator owns all device memory, or loops that cannot pay for
  * cudaMalloc's device-wide synchronisation.  At most 1,048,576 blocks per
  * call (ceil(nbEle/blockSize); 134,217,728 values at blockSize 128), else

@@ -53,7 +53,7 @@ static WsLayout ws_layout(int layout, int dtype, size_t n, int bs) {
     size_t off = 0;
     L.hdr = off; off += 4096;
     L.st32 = off; off += a256(4 * (L.status_tiles + 16));
-    L.st = off; off += a256(3 * 8 * L.status_tiles);
+    L.st = off; off += a256(8 * (3 * L.status_tiles > blocked_status_words(nb) ? 3 * L.status_tiles : blocked_status_words(nb)));
     L.st2 = off; off += a256(3 * 8 * L.status2_tiles);
     L.partials = off; off += a256(4096 * 24);
     L.o = off; off += a256(2 * L.blocks);

@@ -113,7 +113,7 @@ __device__ __forceinline__ bool lane_vec_ok(const void* block_base) {
 // warp instruction and the per-block work is replicated G times, not 32.
 
 template <typename T> struct EncCfg;
-template <> struct EncCfg<float> { static constexpr int E = 16; };
+template <> struct EncCfg<float> { static constexpr int E = 16; };    // values per lane
 template <> struct EncCfg<double> { static constexpr int E = 8; };
 
 template <int G, typename V>
@@ -133,16 +133,54 @@ __device__ __forceinline__ V seg_inclusive_sum(V v) {
     return v;
 }
 
+// Chunked lane layout.  A block is split into chunks of 4 values (one lead
+// byte each); lane sl of a G-lane segment owns chunks sl, sl+G, sl+2G, ...
+// so consecutive lanes touch consecutive chunks (no shared-memory bank
+// conflicts) while each chunk stays contiguous for the XOR chain.
+template <typename T, int G>
+struct Chunks {
+    static constexpr int E = EncCfg<T>::E;
+    static constexpr int NC = E / 4;                  // chunks per lane
+    static constexpr int CB = 4 * (int)sizeof(T);     // bytes per chunk
+    // first value of the lane's k-th chunk
+    static __device__ __forceinline__ int first(int sl, int k) { return 4 * (sl + k * G); }
+};
+
+template <typename T, int G>
+__device__ __forceinline__ void load_chunks(const T* xs, int len, bool vec, T (&v)[EncCfg<T>::E]) {
+    using C = Chunks<T, G>;
+    const int sl = (int)(lane_id() & (G - 1));
+#pragma unroll
+    for (int k = 0; k < C::NC; k++) {
+        const int f = C::first(sl, k);
+        if (vec && f + 4 <= len) {
+            if constexpr (sizeof(T) == 4) {
+                const float4 q = *(const float4*)(xs + f);
+                v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+            } else {
+                const double2 a = *(const double2*)(xs + f), b = *(const double2*)(xs + f + 2);
+                v[4 * k] = a.x; v[4 * k + 1] = a.y; v[4 * k + 2] = b.x; v[4 * k + 3] = b.y;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++) v[4 * k + i] = f + i < len ? xs[f + i] : (T)0;
+        }
+    }
+}
+
 // Segment-wide min/max with the reference's sequential semantics
 // (szx/src/szx_float.cc:322-345): the first value reaching an extreme wins,
 // NaNs are skipped unless the block's first value is NaN.
-template <typename T, int E, int G>
-__device__ __forceinline__ void seg_minmax(const T (&v)[E], int nv, T& mn, T& mx) {
+template <typename T, int G>
+__device__ __forceinline__ void seg_minmax(const T (&v)[EncCfg<T>::E], int len, T& mn, T& mx) {
+    using C = Chunks<T, G>;
+    constexpr int E = C::E;
+    const int sl = (int)(lane_id() & (G - 1));
     if constexpr (sizeof(T) == 4) {
         float lo = __builtin_huge_valf(), hi = -__builtin_huge_valf();
 #pragma unroll
         for (int e = 0; e < E; e++)
-            if (e < nv) { lo = fminf(lo, v[e]); hi = fmaxf(hi, v[e]); }
+            if (C::first(sl, e / 4) + (e & 3) < len) { lo = fminf(lo, v[e]); hi = fmaxf(hi, v[e]); }
 #pragma unroll
         for (int d = G / 2; d > 0; d >>= 1) {
             lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, d, G));
@@ -155,7 +193,7 @@ __device__ __forceinline__ void seg_minmax(const T (&v)[E], int nv, T& mn, T& mx
 #pragma unroll
         for (int e = 0; e < E; e++) {
             unsigned long long u = (unsigned long long)__double_as_longlong(v[e]);
-            bool ok = e < nv && (u & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
+            bool ok = C::first(sl, e / 4) + (e & 3) < len && (u & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
             long long k = (long long)(u ^ ((unsigned long long)((long long)u >> 63) & 0x7FFFFFFFFFFFFFFFull));
             if (ok) { lo = k < lo ? k : lo; hi = k > hi ? k : hi; }
         }
@@ -172,21 +210,28 @@ __device__ __forceinline__ void seg_minmax(const T (&v)[E], int nv, T& mn, T& mx
         mn = inv(lo);
         mx = inv(hi);
     }
-    // a zero extreme takes the sign of the block's first zero (all lanes take part)
-    int ze = E;
-    T zv = 0;
+    // a zero extreme takes the sign of the block's first zero; only warps
+    // that met one pay for the search
+    if (__any_sync(0xffffffffu, mn == (T)0 || mx == (T)0)) {
+        int zi = 1 << 30;
+        T zv = 0;
 #pragma unroll
-    for (int e = E - 1; e >= 0; e--)
-        if (e < nv && v[e] == (T)0) { ze = e; zv = v[e]; }
-    const unsigned lane = lane_id();
-    const unsigned seg0 = lane & ~(unsigned)(G - 1);
-    const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
-    const unsigned m = __ballot_sync(0xffffffffu, ze < E) & segmask;
-    const int fl = m ? __ffs(m) - 1 : (int)seg0;
-    const T first = __shfl_sync(0xffffffffu, zv, fl);
-    if (m) {
-        if (mn == (T)0) mn = first;
-        if (mx == (T)0) mx = first;
+        for (int e = E - 1; e >= 0; e--) {
+            const int idx = C::first(sl, e / 4) + (e & 3);
+            if (idx < len && v[e] == (T)0 && idx < zi) { zi = idx; zv = v[e]; }
+        }
+        int best = zi;
+#pragma unroll
+        for (int d = G / 2; d > 0; d >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, d, G));
+        const unsigned m = __ballot_sync(0xffffffffu, zi == best && zi < (1 << 30));
+        const unsigned seg0 = lane_id() & ~(unsigned)(G - 1);
+        const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
+        const unsigned mm = m & segmask;
+        const T first = __shfl_sync(0xffffffffu, zv, mm ? __ffs(mm) - 1 : (int)seg0);
+        if (mm) {
+            if (mn == (T)0) mn = first;
+            if (mx == (T)0) mx = first;
+        }
     }
     const T x0 = __shfl_sync(0xffffffffu, v[0], 0, G);
     if (isnan(x0)) { mn = x0; mx = x0; }
@@ -195,7 +240,7 @@ __device__ __forceinline__ void seg_minmax(const T (&v)[E], int nv, T& mn, T& mx
 // ------------------------------------------------------------------ encode
 
 struct EncArgs {
-    TileStatus32 st32;
+    unsigned long long* st64;    // tile status, [ntiles + 4]
     const void* x;
     unsigned long long n, nb, ntiles;
     int bs;
@@ -204,9 +249,9 @@ struct EncArgs {
     const CodecParams* params;   // when set, params->eb overrides eb
     uint8_t* payload;            // fixed position of the payload region
     unsigned long long payload_cap;
-    uint16_t* o_scr;
-    uint32_t* m_scr;
-    uint8_t* s_scr;
+    uint16_t* size_blk;          // [nb] payload bytes by block (0: constant)
+    uint32_t* med_blk;           // [nb] stored median by block
+    uint8_t* s_scr;              // state bits
     unsigned long long* tile_ctr;
     int* err;
     Totals* tot;
@@ -245,22 +290,24 @@ __device__ __forceinline__ void cta_copy_out(const uint8_t* stage, uint32_t sh, 
 }
 
 // One pass over the input, software-pipelined over three tile buffers:
-//   load tile t+2 (TMA bulk copy)  |  pass A of tile t+1, publish its aggregate
-//                                  |  resolve tile t's prefix, pass B of tile t
-// Pass A (a segment per block): statistics, state, reqLength, the shifted
-// words (written back over the input in shared memory), lead codes and
-// stored-byte counts.  Pass B emits the payloads of the whole tile into one
-// staging buffer with byte stores; the CTA then writes the tile's contiguous
-// byte range with aligned 16-byte stores.  Publishing tile t+1's aggregate
-// before resolving tile t means predecessors have normally published long
-// before a tile's look-back walks over them.
+//   load tile t+2 (TMA bulk copy)  |  pass A of tile t+1, publish its byte count
+//                                  |  resolve tile t's offset, pass B of tile t
+// Pass A (a segment of G lanes per block): statistics, state, reqLength, the
+// shifted words (written back over the input in shared memory), lead codes
+// and stored-byte counts.  Pass B emits the payloads of the whole tile into
+// one staging buffer with byte stores; the CTA then writes the tile's
+// contiguous byte range with aligned 16-byte stores.  Publishing tile t+1's
+// count before resolving tile t means predecessors have normally published
+// long before a tile's look-back walks over them.
 template <typename T, int G>
 __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     using TL = EncTile<T, G>;
+    using C = Chunks<T, G>;
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
     constexpr int E = TL::E;
+    constexpr int NC = C::NC;
     constexpr int TB = TL::kBlocks;
     constexpr int BPW = TL::kBpw;
     constexpr int NGRP = TB / BPW;   // block groups per tile
@@ -268,11 +315,10 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     uint8_t* bufs = dsm;
     uint8_t* stg = dsm + 3 * TL::kIn;
     __shared__ unsigned long long bar[3];
-    __shared__ uint32_t s_size[2][TB], s_med[2][TB], s_medf[2][TB], s_loc[2][TB], s_lrank[2][TB];
+    __shared__ uint32_t s_size[2][TB], s_med[2][TB], s_loc[2][TB];
     __shared__ uint8_t s_state[2][TB], s_req[2][TB];
-    __shared__ uint32_t s_codes[2][TL::kSlots];
-    __shared__ uint8_t s_lb[2][TL::kSlots];
-    __shared__ uint32_t s_agg[2][2];
+    __shared__ uint32_t s_codes[2][TL::kSlots], s_cnt[2][TL::kSlots];
+    __shared__ uint32_t s_agg[2];
     __shared__ unsigned long long s_base;
     __shared__ long long s_next;
     __shared__ int s_skip;
@@ -284,6 +330,7 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     const long long nt = (long long)a.ntiles;
     const unsigned long long tile_elems = (unsigned long long)TB * a.bs;
     const bool tma_ok = ((uintptr_t)x & 15) == 0;
+    const bool vec = ((a.bs * (int)sizeof(T)) & 15) == 0;   // every block starts 16-byte aligned
     if (threadIdx.x == 0) {
         for (int i = 0; i < 3; i++) mbar_init(&bar[i], 1);
         mbar_fence_init();
@@ -321,26 +368,25 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         __syncthreads();
         return s_next;
     };
+    auto block_len = [&](long long t, int lb) {
+        const unsigned long long b = (unsigned long long)t * TB + lb;
+        if (b >= a.nb) return 0;
+        const unsigned long long rem = a.n - b * (unsigned long long)a.bs;
+        return rem < (unsigned long long)a.bs ? (int)rem : a.bs;
+    };
 
-    // ---- pass A of tile t held in buffer `which`, results in slot `sl2`;
-    // then warp 0 scans the tile and publishes its aggregate.
+    // ---- pass A of tile t (buffer `which`), results in `slot`; warp 0 then
+    // scans the tile and publishes its byte count
     auto pass_a = [&](long long t, int which, int slot) {
         T* xt = (T*)(bufs + which * TL::kIn);
         for (int grp = warp; grp < NGRP; grp += kEncWarps) {
             const int lb = grp * BPW + seg;
-            const unsigned long long b = (unsigned long long)t * TB + lb;
-            int len = 0;
-            if (b < a.nb) {
-                const unsigned long long rem = a.n - b * (unsigned long long)a.bs;
-                len = rem < (unsigned long long)a.bs ? (int)rem : a.bs;
-            }
+            const int len = block_len(t, lb);
             T* xs = xt + (size_t)lb * a.bs;
-            int nv = len - sl * E;
-            nv = nv < 0 ? 0 : (nv > E ? E : nv);
             T v[E];
-            load_lane<T, E>(xs + sl * E, nv, lane_vec_ok<T, E>(xs), v);
+            load_chunks<T, G>(xs, len, vec, v);
             T mn, mx;
-            seg_minmax<T, E, G>(v, nv, mn, mx);
+            seg_minmax<T, G>(v, len, mn, mx);
             int state;
             float radius_f, median_f;
             if constexpr (sizeof(T) == 4) {
@@ -371,50 +417,77 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
             T med;
             if constexpr (sizeof(T) == 4) med = __uint_as_float(med_bits);
             else med = xf2d(median_f);
-            // shifted words, lead codes, stored-byte counts (szx/src/szx_float.cc:88-216)
-            T d[E];
-            bool bad = false;
-#pragma unroll
-            for (int e = 0; e < E; e++) {
-                d[e] = EL::sub(v[e], med);
-                bad |= d[e] != d[e];
-            }
-            if (__any_sync(0xffffffffu, bad)) {
-#pragma unroll
-                for (int e = 0; e < E; e++) d[e] = xsub(v[e], med);
-            }
+            // shifted words (szx/src/szx_float.cc:88-92)
             U cur[E];
+            {
+                T d[E];
+                bool bad = false;
 #pragma unroll
-            for (int e = 0; e < E; e++) cur[e] = EL::bits(d[e]) >> s;
-            U prev = __shfl_up_sync(0xffffffffu, cur[E - 1], 1, G);
-            if (sl == 0) prev = 0;
-            uint32_t codes = 0, lane_bytes = 0;
-#pragma unroll
-            for (int e = 0; e < E; e++) {
-                const U xr = cur[e] ^ (e ? cur[e - 1] : prev);
-                int lz;
-                if constexpr (sizeof(T) == 4) lz = __clz(xr | 0xFFu) >> 3;
-                else lz = __clzll((long long)(xr | 0xFFFFFFFFFFull)) >> 3;
-                const int c = R - lz;
-                if (e < nv) {
-                    codes |= (uint32_t)lz << (2 * (E - 1 - e));
-                    lane_bytes += c > 0 ? c : 0;
+                for (int e = 0; e < E; e++) {
+                    d[e] = EL::sub(v[e], med);
+                    bad |= d[e] != d[e];
                 }
+                if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+                    for (int e = 0; e < E; e++) d[e] = xsub(v[e], med);
+                }
+#pragma unroll
+                for (int e = 0; e < E; e++) cur[e] = EL::bits(d[e]) >> s;
+            }
+            // lead codes and stored-byte counts (szx/src/szx_float.cc:94-113), per chunk
+            uint32_t codes = 0, cnts = 0;
+            U last_prev = 0;
+#pragma unroll
+            for (int k = 0; k < NC; k++) {
+                // value before this chunk: the previous lane's chunk k, or for
+                // lane 0 the last lane's chunk k-1 (zero before the block)
+                const U up = __shfl_up_sync(0xffffffffu, cur[4 * k + 3], 1, G);
+                const U wrap = __shfl_sync(0xffffffffu, last_prev, G - 1, G);
+                U prev = sl ? up : (k ? wrap : (U)0);
+                last_prev = cur[4 * k + 3];
+                const int f = C::first(sl, k);
+                uint32_t byte = 0, nbytes = 0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const U xr = cur[4 * k + i] ^ (i ? cur[4 * k + i - 1] : prev);
+                    int lz;
+                    if constexpr (sizeof(T) == 4) lz = __clz(xr | 0xFFu) >> 3;
+                    else lz = __clzll((long long)(xr | 0xFFFFFFFFFFull)) >> 3;
+                    const bool in = f + i < len;
+                    byte = (byte << 2) | (in ? (uint32_t)lz : 0u);
+                    const int c = R - lz;
+                    nbytes += (in && c > 0) ? c : 0;
+                }
+                codes |= byte << (8 * k);
+                cnts |= nbytes << (8 * k);
             }
             // keep the shifted words for pass B, over the input values
-            U* cs = (U*)(xs + sl * E);
+            U* cs = (U*)xs;
 #pragma unroll
-            for (int e = 0; e < E; e++)
-                if (e < nv) cs[e] = cur[e];
+            for (int k = 0; k < NC; k++) {
+                const int f = C::first(sl, k);
+                if (vec && f + 4 <= len) {
+                    if constexpr (sizeof(T) == 4) {
+                        *(uint4*)(cs + f) = make_uint4(cur[4 * k], cur[4 * k + 1], cur[4 * k + 2], cur[4 * k + 3]);
+                    } else {
+                        *(ulonglong2*)(cs + f) = make_ulonglong2(cur[4 * k], cur[4 * k + 1]);
+                        *(ulonglong2*)(cs + f + 2) = make_ulonglong2(cur[4 * k + 2], cur[4 * k + 3]);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        if (f + i < len) cs[f + i] = cur[4 * k + i];
+                }
+            }
             s_codes[slot][lb * G + sl] = codes;
-            s_lb[slot][lb * G + sl] = (uint8_t)lane_bytes;
+            s_cnt[slot][lb * G + sl] = cnts;
+            const uint32_t lane_bytes = (cnts & 0xFF) + ((cnts >> 8) & 0xFF) + ((cnts >> 16) & 0xFF) + (cnts >> 24);
             const uint32_t size = 5 + (uint32_t)((len + 3) / 4) + seg_sum<G>(lane_bytes);
             if (sl == 0) {
                 const int st = len ? state : 2;
                 s_state[slot][lb] = (uint8_t)st;
                 s_size[slot][lb] = st == 1 ? size : 0;
                 s_med[slot][lb] = state == 1 ? med_bits : __float_as_uint(median_f);
-                s_medf[slot][lb] = __float_as_uint(median_f);
                 s_req[slot][lb] = (uint8_t)reqLength;
             }
         }
@@ -422,25 +495,23 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         if (warp == 0) {
             const bool in0 = lane < TB, in1 = lane + 32 < TB;
             const uint32_t sz0 = in0 ? s_size[slot][lane] : 0, sz1 = in1 ? s_size[slot][lane + 32] : 0;
-            const uint32_t nn0 = in0 && s_state[slot][lane] == 1, nn1 = in1 && s_state[slot][lane + 32] == 1;
-            const uint32_t i0 = warp_inclusive_sum(sz0), j0 = warp_inclusive_sum(nn0);
-            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), u0 = __shfl_sync(0xffffffffu, j0, 31);
-            const uint32_t i1 = warp_inclusive_sum(sz1) + t0, j1 = warp_inclusive_sum(nn1) + u0;
-            const uint32_t agg_sz = __shfl_sync(0xffffffffu, i1, 31), agg_nn = __shfl_sync(0xffffffffu, j1, 31);
-            if (in0) { s_loc[slot][lane] = i0 - sz0; s_lrank[slot][lane] = j0 - nn0; }
-            if (in1) { s_loc[slot][lane + 32] = i1 - sz1; s_lrank[slot][lane + 32] = j1 - nn1; }
-            if (lane == 0) { s_agg[slot][0] = agg_sz; s_agg[slot][1] = agg_nn; }
-            lookback_publish(a.st32, t, agg_sz, agg_nn);
+            const uint32_t i0 = warp_inclusive_sum(sz0);
+            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31);
+            const uint32_t i1 = warp_inclusive_sum(sz1) + t0;
+            const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
+            if (in0) s_loc[slot][lane] = i0 - sz0;
+            if (in1) s_loc[slot][lane + 32] = i1 - sz1;
+            if (lane == 0) s_agg[slot] = agg;
+            prefix_publish(a.st64, t, agg);
         }
     };
 
-    // ---- warp 0: prefix of tile t (slot), per-block metadata
+    // ---- warp 0: offset of tile t, per-block sizes / medians / state bits
     auto resolve = [&](long long t, int slot) {
         if (warp != 0) return;
-        const uint32_t agg_sz = s_agg[slot][0], agg_nn = s_agg[slot][1];
-        unsigned long long base_sz, base_nn;
-        lookback_resolve(a.st32, t, agg_sz, agg_nn, &base_sz, &base_nn, a.err);
-        const bool cap_ok = base_sz + agg_sz <= a.payload_cap;
+        const uint32_t agg = s_agg[slot];
+        const unsigned long long base = prefix_resolve(a.st64, t, agg, a.err);
+        const bool cap_ok = base + agg <= a.payload_cap;
         const unsigned long long tb0 = (unsigned long long)t * TB;
         uint32_t m01[2];
 #pragma unroll
@@ -449,9 +520,8 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
             const bool in = lb < TB;
             const int st = in ? s_state[slot][lb] : 2;
             if (in && st != 2) {
-                const unsigned long long rank = base_nn + s_lrank[slot][lb];
-                if (st == 1) a.o_scr[rank] = (uint16_t)s_size[slot][lb];
-                else a.m_scr[tb0 + lb - rank] = s_med[slot][lb];
+                a.size_blk[tb0 + lb] = (uint16_t)s_size[slot][lb];
+                a.med_blk[tb0 + lb] = s_med[slot][lb];
             }
             m01[h] = __ballot_sync(0xffffffffu, in && st == 1);
         }
@@ -462,11 +532,9 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
 #pragma unroll
             for (int k = 0; k < TB / 8; k++) sbp[k] = (uint8_t)((k < 4 ? r0 : r1) >> (24 - 8 * (k & 3)));
             if (!cap_ok) atomicExch(a.err, kErrCapacity);
-            if (t == nt - 1) {
-                a.tot->payload_bytes = base_sz + agg_sz;
-                a.tot->nnc = base_nn + agg_nn;
-            }
-            s_base = base_sz;
+            atomicAdd(&a.tot->nnc, (unsigned long long)(__popc(m01[0]) + __popc(m01[1])));
+            if (t == nt - 1) a.tot->payload_bytes = base + agg;
+            s_base = base;
             s_skip = !cap_ok;
         }
     };
@@ -479,21 +547,20 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         for (int grp = warp; grp < NGRP; grp += kEncWarps) {
             const int lb = grp * BPW + seg;
             const bool active = s_state[slot][lb] == 1;
-            const unsigned long long b = (unsigned long long)t * TB + lb;
-            int len = 0;
-            if (b < a.nb) {
-                const unsigned long long rem = a.n - b * (unsigned long long)a.bs;
-                len = rem < (unsigned long long)a.bs ? (int)rem : a.bs;
-            }
-            int nv = len - sl * E;
-            nv = nv < 0 ? 0 : (nv > E ? E : nv);
+            const int len = block_len(t, lb);
             const int reqLength = s_req[slot][lb];
             int R, s;
             split_reqlen(reqLength, &R, &s);
             (void)s;
             const uint32_t codes = s_codes[slot][lb * G + sl];
-            const uint32_t lbytes = s_lb[slot][lb * G + sl];
-            const uint32_t incl = seg_inclusive_sum<G>(lbytes);
+            const uint32_t cnts = s_cnt[slot][lb * G + sl];
+            // all chunk offsets from one scan of four packed 16-bit counts
+            unsigned long long pk = 0;
+#pragma unroll
+            for (int k = 0; k < NC; k++) pk |= (unsigned long long)((cnts >> (8 * k)) & 0xFF) << (16 * k);
+            const unsigned long long incl = seg_inclusive_sum<G>(pk);
+            const unsigned long long tot = __shfl_sync(0xffffffffu, incl, G - 1, G);
+            const unsigned long long excl = incl - pk;
             if (!active) continue;
             uint8_t* p = stg + sh + s_loc[slot][lb];
             const int Lb = (len + 3) / 4;
@@ -505,31 +572,35 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
                 p[3] = (uint8_t)(mb >> 8);
                 p[4] = (uint8_t)mb;
             }
-            // lead codes: 4 per byte, MSB first (szx/src/szx_TypeManager.cc:198-273)
-#pragma unroll
-            for (int j = 0; j < E / 4; j++) {
-                const int bi = sl * (E / 4) + j;
-                if (bi < Lb) p[5 + bi] = (uint8_t)(codes >> (8 * (E / 4 - 1 - j)));
-            }
-            // mid bytes: bytes [W-R .. W-1-lead] of each shifted word, ascending
-            uint8_t* q = p + 5 + Lb + (incl - lbytes);
-            const U* cs = (const U*)(xt + (size_t)lb * a.bs + sl * E);
+            const U* cs = (const U*)(xt + (size_t)lb * a.bs);
             const int low = 8 * (W - R);
+            uint32_t before = 0;   // bytes of the earlier chunk rounds
 #pragma unroll
-            for (int e = 0; e < E; e++) {
-                if (e < nv) {
-                    const int ld = (codes >> (2 * (E - 1 - e))) & 3;
-                    const int c = R - ld;
-                    const U ev = cs[e] >> low;
+            for (int k = 0; k < NC; k++) {
+                const int f = C::first(sl, k);
+                const int ci = f >> 2;   // chunk index = lead byte index
+                // lead codes: 4 per byte, MSB first (szx/src/szx_TypeManager.cc:198-273)
+                if (ci < Lb) p[5 + ci] = (uint8_t)(codes >> (8 * k));
+                uint8_t* q = p + 5 + Lb + before + (uint32_t)((excl >> (16 * k)) & 0xFFFF);
+                before += (uint32_t)((tot >> (16 * k)) & 0xFFFF);
+                const uint32_t byte = (codes >> (8 * k)) & 0xFF;
+                // mid bytes: bytes [W-R .. W-1-lead] of each shifted word, ascending
 #pragma unroll
-                    for (int j = 0; j < W; j++)
-                        if (j < c) q[j] = (uint8_t)(ev >> (8 * j));
-                    q += c > 0 ? c : 0;
+                for (int i = 0; i < 4; i++) {
+                    if (f + i < len) {
+                        const int ld = (byte >> (6 - 2 * i)) & 3;
+                        const int c = R - ld;
+                        const U ev = cs[f + i] >> low;
+#pragma unroll
+                        for (int j = 0; j < W; j++)
+                            if (j < c) q[j] = (uint8_t)(ev >> (8 * j));
+                        q += c > 0 ? c : 0;
+                    }
                 }
             }
         }
         __syncthreads();
-        if (!s_skip) cta_copy_out(stg, sh, s_agg[slot][0], a.payload + base);
+        if (!s_skip) cta_copy_out(stg, sh, s_agg[slot], a.payload + base);
     };
 
     // ---- pipeline
@@ -562,57 +633,141 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     }
 }
 
-// Header, size index, state bits and constant medians (szx/src/szx_float.cc:1437-1483).
-__global__ void k_blocked_assemble(int layout, unsigned long long bs, unsigned long long nb, uint8_t* out,
-                                   const Totals* tot, const uint16_t* o_scr, const uint32_t* m_scr,
-                                   const uint8_t* s_scr, StreamResult* res, const CodecParams* params, float eb_abs,
-                                   const int* err) {
-    const unsigned long long nnc = tot->nnc, nc = nb - nnc, sb = (nb + 7) / 8;
-    const bool ra = layout != kBlocked;
+// Header, size index, state bits and medians (szx/src/szx_float.cc:1437-1483).
+// The encoder leaves payload sizes and medians by block index; this kernel
+// compacts them: an assemble tile covers kAsmWords state words (32 blocks
+// each), the non-constant rank of its first block comes from an inline-prefix
+// look-back over the tiles' popcounts, and each block then writes its size
+// (non-constant, by rank) or its median (constant, by constant rank).
+constexpr int kAsmThreads = 256;
+constexpr int kAsmWords = (int)(kAsmBlocksPerTile / 32);
+
+struct AsmArgs {
+    int layout;
+    unsigned long long bs, nb;
+    uint8_t* out;
+    const Totals* tot;
+    const uint16_t* size_blk;
+    const uint32_t* med_blk;
+    const uint8_t* s_scr;
+    unsigned long long* st;      // assemble tile status, [tiles + 4]
+    unsigned long long* ctr;     // [0] tile counter, [1] finished CTAs
+    StreamResult* res;
+    const CodecParams* params;
+    float eb_abs;
+    int* err;
+};
+
+__global__ void __launch_bounds__(kAsmThreads) k_blocked_assemble(AsmArgs a) {
+    __shared__ uint32_t s_word[kAsmWords], s_pre[kAsmWords];
+    __shared__ uint32_t s_wsum[kAsmThreads / 32];
+    __shared__ long long s_t;
+    __shared__ unsigned long long s_base;
+    __shared__ int s_last;
+    const unsigned long long nb = a.nb, nnc = a.tot->nnc, nc = nb - nnc, sb = (nb + 7) / 8;
+    const bool ra = a.layout != kBlocked;
     const unsigned long long hdr = ra ? 20 : 13;
     const unsigned long long shift = ra ? 2 * nnc : 4 * nnc;
-    uint8_t* s = out + shift;
+    uint8_t* s = a.out + shift;
     uint8_t* O = s + hdr;
     uint8_t* R = O + (ra ? 2 * nnc : 0);
-    uint8_t* P = R + sb;
-    const unsigned long long tid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned long long nthr = (unsigned long long)gridDim.x * blockDim.x;
-    unsigned long long m = nnc > nc ? nnc : nc;
-    m = m > sb ? m : sb;
-    for (unsigned long long i = tid; i < m; i += nthr) {
-        if (ra && i < nnc) {
-            uint16_t v = o_scr[i];
-            O[2 * i] = (uint8_t)v;
-            O[2 * i + 1] = (uint8_t)(v >> 8);
-        }
-        if (i < sb) R[i] = s_scr[i];
-        if (i < nc) {
-            uint32_t v = m_scr[i];
-            if (layout == kRandomAccessNative) {
-                P[4 * i] = (uint8_t)v; P[4 * i + 1] = (uint8_t)(v >> 8);
-                P[4 * i + 2] = (uint8_t)(v >> 16); P[4 * i + 3] = (uint8_t)(v >> 24);
-            } else {
-                P[4 * i] = (uint8_t)(v >> 24); P[4 * i + 1] = (uint8_t)(v >> 16);
-                P[4 * i + 2] = (uint8_t)(v >> 8); P[4 * i + 3] = (uint8_t)v;
+    uint8_t* M = R + sb;
+    const bool o_aligned = ((uintptr_t)O & 1) == 0;
+    const unsigned long long nw = (nb + 31) / 32;
+    const long long ntiles = (long long)((nw + kAsmWords - 1) / kAsmWords);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (;;) {
+        if (tid == 0) s_t = (long long)atomicAdd(a.ctr, 1ull);
+        __syncthreads();
+        const long long t = s_t;
+        if (t >= ntiles) break;
+        const unsigned long long w = (unsigned long long)t * kAsmWords + tid;
+        uint32_t word = 0;
+        if (tid < kAsmWords && w < nw) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const unsigned long long bi = 4 * w + j;
+                const uint32_t byte = bi < sb ? (uint32_t)a.s_scr[bi] : 0u;
+                word = (word << 8) | byte;
+                if (bi < sb) R[bi] = (uint8_t)byte;
             }
         }
+        const uint32_t pc = __popc(word);
+        const uint32_t incl = warp_inclusive_sum(pc);
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        uint32_t wpre = 0, agg = 0;
+#pragma unroll
+        for (int k = 0; k < kAsmThreads / 32; k++) {
+            const uint32_t v = s_wsum[k];
+            wpre += k < warp ? v : 0u;
+            agg += v;
+        }
+        if (tid < kAsmWords) {
+            s_word[tid] = word;
+            s_pre[tid] = wpre + incl - pc;
+        }
+        if (warp == 0) {
+            prefix_publish(a.st, t, agg);
+            const unsigned long long base = prefix_resolve(a.st, t, agg, a.err);
+            if (lane == 0) s_base = base;
+        }
+        __syncthreads();
+        const unsigned long long base = s_base;
+        const unsigned long long b0 = (unsigned long long)t * kAsmWords * 32;
+#pragma unroll 4
+        for (int k = 0; k < kAsmWords * 32 / kAsmThreads; k++) {
+            const int lb = k * kAsmThreads + tid;
+            const unsigned long long b = b0 + lb;
+            if (b >= nb) break;
+            const uint32_t wd = s_word[lb >> 5];
+            const int bit = lb & 31;
+            const unsigned long long rank = base + s_pre[lb >> 5] + (bit ? __popc(wd >> (32 - bit)) : 0);
+            if ((wd >> (31 - bit)) & 1u) {
+                if (ra) {
+                    const uint16_t v = a.size_blk[b];
+                    if (o_aligned) {
+                        *(uint16_t*)(O + 2 * rank) = v;   // little-endian u16
+                    } else {
+                        O[2 * rank] = (uint8_t)v;
+                        O[2 * rank + 1] = (uint8_t)(v >> 8);
+                    }
+                }
+            } else {
+                const uint32_t v = a.med_blk[b];
+                uint8_t* q = M + 4 * (b - rank);
+                if (a.layout == kRandomAccessNative) {
+                    q[0] = (uint8_t)v; q[1] = (uint8_t)(v >> 8); q[2] = (uint8_t)(v >> 16); q[3] = (uint8_t)(v >> 24);
+                } else {
+                    q[0] = (uint8_t)(v >> 24); q[1] = (uint8_t)(v >> 16); q[2] = (uint8_t)(v >> 8); q[3] = (uint8_t)v;
+                }
+            }
+        }
+        __syncthreads();
     }
+    // the last CTA to finish writes the header and the result record
     if (tid == 0) {
+        __threadfence();
+        s_last = atomicAdd(&a.ctr[1], 1ull) == (unsigned long long)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last && tid == 0) {
+        __threadfence();
         s[0] = 1; s[1] = 1; s[2] = 1; s[3] = ra ? 1 : 0;
         if (ra) {
-            for (int k = 0; k < 8; k++) s[4 + k] = (uint8_t)(bs >> (56 - 8 * k));
+            for (int k = 0; k < 8; k++) s[4 + k] = (uint8_t)(a.bs >> (56 - 8 * k));
             for (int k = 0; k < 8; k++) s[12 + k] = (uint8_t)(nc >> (56 - 8 * k));
         } else {
-            s[4] = (uint8_t)bs;
+            s[4] = (uint8_t)a.bs;
             for (int k = 0; k < 8; k++) s[5 + k] = (uint8_t)(nc >> (56 - 8 * k));
         }
         StreamResult r;
         r.offset = shift;
-        r.size = hdr + (ra ? 2 * nnc : 0) + sb + 4 * nc + tot->payload_bytes;
+        r.size = hdr + (ra ? 2 * nnc : 0) + sb + 4 * nc + a.tot->payload_bytes;
         r.nb_const = nc;
-        r.eb = params ? params->eb : eb_abs;
-        r.status = *err;
-        *res = r;
+        r.eb = a.params ? a.params->eb : a.eb_abs;
+        r.status = *(volatile int*)a.err;
+        *a.res = r;
     }
 }
 
@@ -643,6 +798,7 @@ static cudaError_t run_encode(EncArgs a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+
 cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
                                   float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s) {
     if (n == 0 || bs < 1 || bs > 256) return cudaErrorInvalidValue;
@@ -651,20 +807,20 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
     const size_t hdr = layout == kBlocked ? 13 : 20;
     const size_t qfix = hdr + sb + 4 * nb;
     if (cap < qfix) return cudaErrorInvalidValue;
-    // tiles hold >= 8 blocks, so nb / 8 + 1 status words cover every tile size
-    const size_t max_tiles = nb / 8 + 1;
+    unsigned long long* st_enc = ws.st_word;
+    unsigned long long* st_asm = ws.st_word + enc_status_words(nb);   // encoder's words first
     cudaError_t e;
-    if ((e = cudaMemsetAsync(ws.st32, 0, sizeof(uint32_t) * (max_tiles + 8), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(ws.counters, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(ws.err, 0, sizeof(int), s)) != cudaSuccess) return e;
+    // status words of both look-backs, then totals / result / error / counters
+    if ((e = cudaMemsetAsync(ws.st_word, 0, 8 * blocked_status_words(nb), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync((uint8_t*)ws.totals, 0, kWsHeaderClear, s)) != cudaSuccess) return e;
     EncArgs a;
-    a.st32 = TileStatus32{ws.st32, ws.st_agg2, ws.st_inc2};
+    a.st64 = st_enc;
     a.x = x; a.n = n; a.nb = nb; a.ntiles = 0; a.bs = bs; a.eb = abs_eb;
     a.omp_stats = layout == kRandomAccessNative;
     a.params = use_params ? ws.params : nullptr;
     a.payload = d_out + qfix;
     a.payload_cap = cap - qfix;
-    a.o_scr = ws.o_scr; a.m_scr = ws.m_scr; a.s_scr = ws.s_scr;
+    a.size_blk = ws.o_scr; a.med_blk = ws.m_scr; a.s_scr = ws.s_scr;
     a.tile_ctr = &ws.counters[0];
     a.err = ws.err;
     a.tot = ws.totals;
@@ -691,12 +847,16 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
         }
     }
     if (e != cudaSuccess) return e;
-    int ag = (int)((nb + 255) / 256);
-    if (ag < 1) ag = 1;
-    if (ag > sm_count() * 4) ag = sm_count() * 4;
+    AsmArgs m;
+    m.layout = layout; m.bs = (unsigned long long)bs; m.nb = nb; m.out = d_out; m.tot = ws.totals;
+    m.size_blk = ws.o_scr; m.med_blk = ws.m_scr; m.s_scr = ws.s_scr;
+    m.st = st_asm; m.ctr = &ws.counters[1]; m.res = ws.result;
+    m.params = use_params ? ws.params : nullptr; m.eb_abs = abs_eb; m.err = ws.err;
+    const size_t tiles = (nb + 32 * kAsmWords - 1) / (32 * kAsmWords);
+    const size_t gmax = (size_t)sm_count() * 4;
+    const int ag = (int)(tiles < gmax ? tiles : gmax);
     TraceScope tr("blocked_assemble", s);
-    k_blocked_assemble<<<ag, 256, 0, s>>>(layout, (unsigned long long)bs, nb, d_out, ws.totals, ws.o_scr, ws.m_scr,
-                                          ws.s_scr, ws.result, use_params ? ws.params : nullptr, abs_eb, ws.err);
+    k_blocked_assemble<<<ag, kAsmThreads, 0, s>>>(m);
     return cudaGetLastError();
 }
 

@@ -82,6 +82,17 @@ struct Workspace {
     size_t status_tiles, status2_tiles, blocks, words, aux_tiles;
 };
 
+// Bytes cleared at the start of every encode, from Workspace::totals up to
+// and including the tile counters (totals, result, headers, error word).
+constexpr size_t kWsHeaderClear = 512;
+// 64-bit look-back status words a blocked encode of nb blocks needs (the
+// encoder's tiles hold >= 8 blocks, the assembler's 2048).  Both arrays start
+// on 32-byte boundaries: the look-back reads them with 16-byte vector loads.
+constexpr size_t kAsmBlocksPerTile = 2048;
+constexpr size_t round4(size_t w) { return (w + 3) & ~size_t(3); }
+constexpr size_t enc_status_words(size_t nb) { return round4(nb / 8 + 9); }
+constexpr size_t blocked_status_words(size_t nb) { return enc_status_words(nb) + round4(nb / kAsmBlocksPerTile + 9); }
+
 size_t ws_bytes(int layout, int dtype, size_t n, int bs);
 Workspace ws_carve(void* base, int layout, int dtype, size_t n, int bs);
 

@@ -9,7 +9,7 @@
 // g_noalloc_scratch below.
 //
 // Cost and limits:
-// * every GPU that loads this library holds kNoAllocBytes (about 8.0 MiB) of
+// * every GPU that loads this library holds kNoAllocBytes (about 7.2 MiB) of
 //   device memory for the array until the process exits;
 // * one call handles at most kNoAllocMaxBlocks = 1,048,576 blocks
 //   (ceil(nbEle / blockSize)), i.e. 134,217,728 values at blockSize 128;
@@ -33,15 +33,13 @@ namespace szxg {
 
 constexpr size_t kNoAllocMaxBlocks = size_t(1) << 20;
 constexpr size_t kNoAllocHeader = 4096;
-constexpr size_t kNoAllocTiles = kNoAllocMaxBlocks / 16 + 2;   // tiles of >= 16 blocks
 constexpr size_t na_a256(size_t x) { return (x + 255) & ~size_t(255); }
-constexpr size_t kNaSt32 = kNoAllocHeader;
-constexpr size_t kNaSt = kNaSt32 + na_a256(4 * (kNoAllocTiles + 16));
-constexpr size_t kNaPartials = kNaSt + na_a256(3 * 8 * kNoAllocTiles);
-constexpr size_t kNaO = kNaPartials + na_a256(4096 * 24);
-constexpr size_t kNaM = kNaO + na_a256(2 * kNoAllocMaxBlocks);
-constexpr size_t kNaS = kNaM + na_a256(4 * kNoAllocMaxBlocks);
-constexpr size_t kNoAllocBytes = kNaS + na_a256(kNoAllocMaxBlocks / 8 + 64);
+constexpr size_t kNaSt = kNoAllocHeader;                                           // look-back status
+constexpr size_t kNaPartials = kNaSt + na_a256(8 * blocked_status_words(kNoAllocMaxBlocks));
+constexpr size_t kNaO = kNaPartials + na_a256(4096 * 24);                         // range-pass partials
+constexpr size_t kNaM = kNaO + na_a256(2 * kNoAllocMaxBlocks);                    // sizes by block
+constexpr size_t kNaS = kNaM + na_a256(4 * kNoAllocMaxBlocks);                    // medians by block
+constexpr size_t kNoAllocBytes = kNaS + na_a256(kNoAllocMaxBlocks / 8 + 64);      // state bits
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -77,15 +75,12 @@ Workspace carve(unsigned char* b) {
     w.result = (StreamResult*)(h + 128);
     w.err = (int*)(h + 448);
     w.counters = (unsigned long long*)(h + 512);
-    w.st32 = (uint32_t*)(b + kNaSt32);
     w.st_word = (unsigned long long*)(b + kNaSt);
-    w.st_agg2 = w.st_word + kNoAllocTiles;
-    w.st_inc2 = w.st_agg2 + kNoAllocTiles;
     w.partials = b + kNaPartials;
     w.o_scr = (uint16_t*)(b + kNaO);
     w.m_scr = (uint32_t*)(b + kNaM);
     w.s_scr = b + kNaS;
-    w.status_tiles = kNoAllocTiles;
+    w.status_tiles = blocked_status_words(kNoAllocMaxBlocks);
     w.blocks = kNoAllocMaxBlocks;
     return w;
 }
