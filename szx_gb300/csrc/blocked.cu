@@ -10,22 +10,24 @@
 //   2-bit lead codes MSB-first | mid bytes.
 //
 // GB300 design
-// * Encode is ONE pass over the input: a CTA takes a tile of blocks from an
-//   atomic tile counter, a warp per block computes min/max (warp shuffles),
-//   state, reqLength and the shifted words in registers, the tile's payload
-//   bytes and non-constant count are placed by a decoupled look-back, and the
-//   payload bytes are emitted from registers into a per-warp shared staging
-//   buffer and stored with aligned 16-byte writes.
+// * Encode is ONE pass over the input.  Persistent CTAs take tiles of blocks
+//   from an atomic counter and pipeline them over three shared-memory buffers
+//   filled by TMA bulk copies.  A block is handled by a segment of G lanes
+//   (16 float / 8 double values per lane) in a chunk-interleaved layout; the
+//   tile's payload bytes are placed by a decoupled look-back whose 64-bit
+//   status words carry the inclusive prefix inline, and each tile's payloads
+//   are emitted into shared memory and written with aligned 16-byte stores.
 // * The payload region is written at a fixed position (as if no block were
-//   non-constant); the stream is then shifted to start 2*nnc (mode 3/4) or
-//   4*nnc (mode 2) bytes into the buffer so that header, index, state bits and
-//   medians (assembled by a small second kernel from per-block scratch) end
+//   non-constant); the stream then starts 2*nnc (mode 3/4) or 4*nnc (mode 2)
+//   bytes into the buffer, so that header, size index, state bits and
+//   medians (compacted from per-block scratch by a small look-back kernel) end
 //   exactly where the payload region begins.  Nothing is ever moved.
-// * Decode scans the size index and the state bits (single-pass look-back),
-//   then a warp per block reconstructs its values: mid-byte offsets come from
-//   a warp prefix sum, and the bytes carried over from previous values (the
-//   top three byte lanes, the only ones a lead code can inherit) from one
-//   packed "last writer" warp scan.
+// * Decode scans the size index and the state bits once (payload offsets by
+//   non-constant rank, rank at each 32-block state word); then a producer
+//   warp per CTA stages each tile's payload range by TMA into a ring of
+//   buffers while eight consumer warps decode G lanes per block, with the
+//   bytes carried from earlier values resolved by a packed "last writer"
+//   scan over 4-value chunks.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -33,77 +35,8 @@ namespace szxg {
 
 constexpr int kEncWarps = 8;
 constexpr int kEncThreads = kEncWarps * 32;
-constexpr int kDecThreads = 256;
 constexpr int kIdxThreads = 256;
 constexpr int kIdxItems = 8;   // items per thread in the index scans
-
-// ------------------------------------------------------------------ lane loads / stores
-
-template <int B> struct RawVec;
-template <> struct RawVec<4> { static __device__ __forceinline__ void ld(const void* p, uint32_t* d) { d[0] = *(const uint32_t*)p; } };
-template <> struct RawVec<8> { static __device__ __forceinline__ void ld(const void* p, uint32_t* d) { uint2 v = *(const uint2*)p; d[0] = v.x; d[1] = v.y; } };
-template <> struct RawVec<16> { static __device__ __forceinline__ void ld(const void* p, uint32_t* d) { uint4 v = *(const uint4*)p; d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w; } };
-
-// Load E consecutive elements of one lane; vector loads when the caller knows
-// the lane's first element is aligned to min(E*sizeof(T), 16) bytes.
-template <typename T, int E>
-__device__ __forceinline__ void load_lane(const T* p, int nv, bool vec_ok, T (&v)[E]) {
-    constexpr int B = E * (int)sizeof(T);
-    if (vec_ok && nv == E) {
-        uint32_t w[B / 4];
-        if constexpr (B >= 16) {
-#pragma unroll
-            for (int i = 0; i < B / 16; i++) RawVec<16>::ld((const uint8_t*)p + 16 * i, w + 4 * i);
-        } else {
-            RawVec<B>::ld(p, w);
-        }
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            if constexpr (sizeof(T) == 4) v[e] = __uint_as_float(w[e]);
-            else v[e] = __longlong_as_double((long long)(((unsigned long long)w[2 * e + 1] << 32) | w[2 * e]));
-        }
-    } else {
-#pragma unroll
-        for (int e = 0; e < E; e++) v[e] = e < nv ? p[e] : (T)0;
-    }
-}
-
-template <typename T, int E>
-__device__ __forceinline__ void store_lane(T* p, int nv, bool vec_ok, const T (&v)[E]) {
-    constexpr int B = E * (int)sizeof(T);
-    if (vec_ok && nv == E) {
-        uint32_t w[B / 4];
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            if constexpr (sizeof(T) == 4) w[e] = __float_as_uint(v[e]);
-            else {
-                unsigned long long u = (unsigned long long)__double_as_longlong(v[e]);
-                w[2 * e] = (uint32_t)u;
-                w[2 * e + 1] = (uint32_t)(u >> 32);
-            }
-        }
-        if constexpr (B >= 16) {
-#pragma unroll
-            for (int i = 0; i < B / 16; i++)
-                *(uint4*)((uint8_t*)p + 16 * i) = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
-        } else if constexpr (B == 8) {
-            *(uint2*)p = make_uint2(w[0], w[1]);
-        } else {
-            *(uint32_t*)p = w[0];
-        }
-    } else {
-#pragma unroll
-        for (int e = 0; e < E; e++)
-            if (e < nv) p[e] = v[e];
-    }
-}
-
-template <typename T, int E>
-__device__ __forceinline__ bool lane_vec_ok(const void* block_base) {
-    constexpr int B = E * (int)sizeof(T);
-    constexpr int A = B < 16 ? B : 16;
-    return ((uintptr_t)block_base % A) == 0;
-}
 
 // ------------------------------------------------------------------ segment helpers
 //
@@ -984,245 +917,404 @@ __global__ void __launch_bounds__(kIdxThreads) k_blocked_index(const uint8_t* s,
     }
 }
 
-// Decode one non-constant block whose payload sits in shared memory at p
-// (any alignment; the 16-byte-aligned buffer around it has >= 16 readable
-// bytes of slack).  Carried bytes: a value inherits its top `lead` bytes from
-// its predecessor, so lane values are first rebuilt with a zero carry, the
-// lane's final top three bytes and the lanes it wrote are scanned across the
-// warp ("last writer wins"), and the real carry is OR-ed into the byte lanes
-// still inherited -- the top min(lead so far) bytes.
-template <typename T, int E>
-__device__ __forceinline__ void dec_block(const uint8_t* p, int len, T* outb) {
+// ------------------------------------------------------------------ decode, per block
+//
+// A segment of G lanes decodes one non-constant block with the encoder's
+// chunk layout: lane sl owns the 4-value chunks sl, sl+G, sl+2G, ... (chunk c
+// = lead byte c of the payload).  Stored bytes are read from the staged
+// payload in shared memory; every value is first rebuilt with a zero carry
+// (its top `lead` bytes come from its predecessor, szx/src/szxd_float.cc:
+// 431-470), then the bytes still inherited from before the chunk are filled in
+// from a "last writer" scan over chunk summaries in block order.
+
+// Chunk summary: [25:24] the smallest lead in the chunk (it wrote the top-3
+// bytes at indices >= that lead), [23:0] the top three bytes of its last value.
+__device__ __forceinline__ uint32_t lw_op(uint32_t a, uint32_t b) {
+    const uint32_t ma = a >> 24, mb = b >> 24;
+    const uint32_t mask = 0xFFFFFFu >> (8 * mb);
+    return ((ma < mb ? ma : mb) << 24) | (a & 0xFFFFFFu & ~mask) | (b & mask);
+}
+constexpr uint32_t kLwNone = 3u << 24;   // writes nothing; the value before a block is zero
+
+template <typename T, int G>
+__device__ __forceinline__ void store_chunks(T* ob, int len, bool vec, const T (&v)[EncCfg<T>::E]) {
+    using C = Chunks<T, G>;
+    const int sl = (int)(lane_id() & (G - 1));
+#pragma unroll
+    for (int k = 0; k < C::NC; k++) {
+        const int f = C::first(sl, k);
+        if (vec && f + 4 <= len) {
+            if constexpr (sizeof(T) == 4) {
+                *(float4*)(ob + f) = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+            } else {
+                *(double2*)(ob + f) = make_double2(v[4 * k], v[4 * k + 1]);
+                *(double2*)(ob + f + 2) = make_double2(v[4 * k + 2], v[4 * k + 3]);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                if (f + i < len) ob[f + i] = v[4 * k + i];
+        }
+    }
+}
+
+template <typename T, int G>
+__device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bool vec) {
+    using C = Chunks<T, G>;
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
+    constexpr int E = C::E;
+    constexpr int NC = C::NC;
     constexpr int TOPSH = 8 * (W - 3);
-    const int lane = (int)lane_id();
+    const int sl = (int)(lane_id() & (G - 1));
     const int reqLength = p[0];
     const uint32_t mb = ((uint32_t)p[1] << 24) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 8) | p[4];
     int R, s;
     split_reqlen(reqLength, &R, &s);
-    const int low = 8 * (W - R);                 // bits below the required bytes
+    R = R < 1 ? 1 : (R > W ? W : R);   // a no-op for valid streams; keeps the shifts defined otherwise
+    const int low = 8 * (W - R);
     const int Lb = (len + 3) / 4;
-    int nv = len - lane * E;
-    nv = nv < 0 ? 0 : (nv > E ? E : nv);
-    uint32_t codes;
-    if constexpr (E == 4) codes = lane < Lb ? p[5 + lane] : 0;
-    else if constexpr (E == 8) codes = ((2 * lane < Lb ? (uint32_t)p[5 + 2 * lane] : 0u) << 8) |
-                                      (2 * lane + 1 < Lb ? (uint32_t)p[6 + 2 * lane] : 0u);
-    else if constexpr (E == 2) codes = lane / 2 < Lb ? ((uint32_t)p[5 + lane / 2] >> ((lane & 1) ? 0 : 4)) & 0xF : 0;
-    else codes = lane / 4 < Lb ? ((uint32_t)p[5 + lane / 4] >> (6 - 2 * (lane & 3))) & 3 : 0;
-    int ld[E], cnt[E];
-    uint32_t lane_bytes = 0;
+    // lead codes (szx/src/szx_TypeManager.cc:198-273: 4 per byte, MSB first) and stored-byte counts
+    uint32_t codes = 0;
+    unsigned long long pk = 0;
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-        ld[e] = (codes >> (2 * (E - 1 - e))) & 3;
-        int c = R - ld[e];
-        cnt[e] = (e < nv && c > 0) ? c : 0;
-        lane_bytes += cnt[e];
+    for (int k = 0; k < NC; k++) {
+        const int c = sl + k * G;
+        const uint32_t code = c < Lb ? (uint32_t)p[5 + c] : 0u;
+        codes |= code << (8 * k);
+        uint32_t n = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int ld = (code >> (6 - 2 * i)) & 3;
+            const int cnt = R - ld;
+            n += (4 * c + i < len && cnt > 0) ? (uint32_t)cnt : 0u;
+        }
+        pk |= (unsigned long long)n << (16 * k);
     }
-    const uint32_t incl = warp_inclusive_sum(lane_bytes);
-    const uint32_t base = (uint32_t)((uintptr_t)p & 15);
-    const uint32_t* buf = (const uint32_t*)((uintptr_t)p - base);
-    uint32_t q = base + 5 + Lb + (incl - lane_bytes);
-    // stored bytes in place, then the zero-carry reconstruction
+    const unsigned long long incl = seg_inclusive_sum<G>(pk);
+    const unsigned long long tot = __shfl_sync(0xffffffffu, incl, G - 1, G);
+    const unsigned long long excl = incl - pk;
+    const uint32_t ph = (uint32_t)((uintptr_t)p & 15);
+    const uint32_t* buf = (const uint32_t*)(p - ph);
     U cur[E];
-    U run = 0;
-    int mld = 3;
+    uint32_t sum[NC];
+    uint32_t before = ph + 5 + (uint32_t)Lb;
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-        const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
-        const uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
-        U sp;
-        if constexpr (sizeof(T) == 4) {
-            sp = (lo & __funnelshift_rc(0xFFFFFFFFu, 0u, 32 - 8 * cnt[e])) << low;   // clamped: cnt 0 -> mask 0
-        } else {
-            const uint32_t w2 = buf[(q >> 2) + 2];
-            const uint32_t hi = __funnelshift_r(w1, w2, (q & 3) * 8);
-            const unsigned long long v = ((unsigned long long)hi << 32) | lo;
-            const unsigned long long m = cnt[e] >= 8 ? ~0ull : ((1ull << (8 * cnt[e])) - 1);
-            sp = (v & m) << low;
-        }
-        q += cnt[e];
-        const U inh = ~(~(U)0 >> (8 * ld[e]));   // the top ld[e] bytes come from the predecessor
-        run = sp | (run & inh);
-        cur[e] = run;
-        if (e < nv) mld = ld[e] < mld ? ld[e] : mld;
-    }
-    // lane summary: top three bytes of its last value, and which of them it wrote
-    const uint32_t wm = nv ? (1u << (3 - mld)) - 1 : 0u;
-    uint32_t sum = (wm << 24) | ((uint32_t)(run >> TOPSH) & 0xFFFFFFu);
+    for (int k = 0; k < NC; k++) {
+        const int c = sl + k * G;
+        uint32_t q = before + (uint32_t)((excl >> (16 * k)) & 0xFFFF);
+        before += (uint32_t)((tot >> (16 * k)) & 0xFFFF);
+        const uint32_t code = (codes >> (8 * k)) & 0xFF;
+        U run = 0;
+        int mld = 3;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        uint32_t o = __shfl_up_sync(0xffffffffu, sum, d);
-        if (lane >= d) {
-            uint32_t bm = sum >> 24;
-            uint32_t wb = (bm & 1) * 0xFFu | (bm & 2) * 0x7F80u | (bm & 4) * 0x3FC000u;
-            sum = (((o >> 24) | bm) << 24) | ((o & 0xFFFFFFu & ~wb) | (sum & 0xFFFFFFu & wb));
+        for (int i = 0; i < 4; i++) {
+            const int ld = (code >> (6 - 2 * i)) & 3;
+            const bool in = 4 * c + i < len;
+            const int cnt = (in && R > ld) ? R - ld : 0;
+            const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
+            const uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
+            U raw;
+            if constexpr (sizeof(T) == 4) {
+                raw = lo;
+            } else {
+                const uint32_t w2 = buf[(q >> 2) + 2];
+                raw = ((unsigned long long)__funnelshift_r(w1, w2, (q & 3) * 8) << 32) | lo;
+            }
+            const U inh = ~(~(U)0 >> (8 * ld));          // top ld bytes: inherited
+            // stored bytes land at [W-R, W-ld); everything above is inherited
+            const U sp = (cnt ? (raw << low) : (U)0) & ~inh;
+            run = sp | (run & inh);
+            cur[4 * k + i] = run;
+            q += (uint32_t)cnt;
+            if (in && ld < mld) mld = ld;
+        }
+        sum[k] = ((uint32_t)mld << 24) | ((uint32_t)(run >> TOPSH) & 0xFFFFFFu);
+    }
+    // last-writer scans: one per chunk round (independent), then the round carries
+    uint32_t inc[NC];
+#pragma unroll
+    for (int k = 0; k < NC; k++) inc[k] = sum[k];
+#pragma unroll
+    for (int d = 1; d < G; d <<= 1) {
+#pragma unroll
+        for (int k = 0; k < NC; k++) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, inc[k], d, G);
+            if (sl >= d) inc[k] = lw_op(o, inc[k]);
         }
     }
-    uint32_t ex = __shfl_up_sync(0xffffffffu, sum, 1);
-    if (lane == 0) ex = 0;   // the value before a block is zero
-    const U carry = (U)(ex & 0xFFFFFFu) << TOPSH;
+    uint32_t carry_in = kLwNone;
     const T med = widen_median<T>(__uint_as_float(mb));
     T v[E];
     bool bad = false;
-    int cm = 3;
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-        cm = ld[e] < cm ? ld[e] : cm;
-        const U keep = ~(~(U)0 >> (8 * cm));       // byte lanes still inherited from before this lane
-        cur[e] = (cur[e] | (carry & keep)) << s;
-        v[e] = EL::add(EL::of(cur[e]), med);
-        bad |= v[e] != v[e];
+    for (int k = 0; k < NC; k++) {
+        uint32_t ex = __shfl_up_sync(0xffffffffu, inc[k], 1, G);
+        if (sl == 0) ex = kLwNone;
+        const uint32_t fin = lw_op(carry_in, ex);
+        carry_in = lw_op(carry_in, __shfl_sync(0xffffffffu, inc[k], G - 1, G));
+        const U carry = (U)(fin & 0xFFFFFFu) << TOPSH;
+        const uint32_t code = (codes >> (8 * k)) & 0xFF;
+        int cm = 3;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int ld = (code >> (6 - 2 * i)) & 3;
+            cm = ld < cm ? ld : cm;
+            const U keep = ~(~(U)0 >> (8 * cm));   // byte lanes inherited from before the chunk
+            const U u = (cur[4 * k + i] | (carry & keep)) << s;
+            cur[4 * k + i] = u;
+            v[4 * k + i] = EL::add(EL::of(u), med);
+            bad |= v[4 * k + i] != v[4 * k + i];
+        }
     }
     if (__any_sync(0xffffffffu, bad)) {
 #pragma unroll
         for (int e = 0; e < E; e++) v[e] = xadd(EL::of(cur[e]), med);
     }
-    store_lane<T, E>(outb + lane * E, nv, lane_vec_ok<T, E>(outb), v);
+    store_chunks<T, G>(ob, len, vec, v);
 }
 
-template <typename T, int E>
-struct DecTile {
-    static constexpr int kMaxPay = 5 + (32 * E + 3) / 4 + (int)sizeof(T) * 32 * E;
-    static constexpr int kBudget = 36 * 1024;
-    static constexpr int kBlocks = (kBudget / kMaxPay) >= 64 ? 64 : (kBudget / kMaxPay) >= 32 ? 32 : 16;
-    static constexpr int kStage = kBlocks * kMaxPay + 64;
+// ------------------------------------------------------------------ decode, pipelined tiles
+//
+// One producer warp per CTA walks the CTA's tiles ahead of the decoders: it
+// reads the tile's state bits and first rank, the payload offsets of its
+// non-constant blocks and the medians of its constant blocks, checks them,
+// and stages the tile's payload bytes (one contiguous range) into a ring of
+// kDecStages shared-memory buffers with a TMA bulk copy.  Eight consumer
+// warps decode a tile per step, G lanes per block, and write the values with
+// 16-byte stores.  Full/empty mbarriers hand the buffers back and forth; every
+// wait is bounded and reports kErrLookback instead of hanging.
+constexpr int kDecWarps = 8;
+constexpr int kDecThreadsP = (kDecWarps + 1) * 32;
+constexpr int kDecStages = 3;
+
+template <typename T, int G>
+struct DecTileV {
+    static constexpr int E = EncCfg<T>::E;
+    static constexpr int kBsMax = G * E;
+    static constexpr int kBpw = 32 / G;
+    static constexpr int kBlocks = kDecWarps * kBpw;     // one segment per consumer warp and tile
+    static constexpr int kMaxPay = 5 + (kBsMax + 3) / 4 + (int)sizeof(T) * kBsMax;
+    // a valid tile's payloads fit kBlocks * kMaxPay; one more kMaxPay + 32
+    // keeps the reads of a corrupt block inside the buffer
+    static constexpr int kStage = (((kBlocks + 1) * kMaxPay + 32) + 15) / 16 * 16;
+    static constexpr int kDynSmem = kDecStages * kStage;
 };
 
-// One CTA per tile of kBlocks blocks: the tile's state bits and non-constant
-// rank come from the index scans, its payloads are one contiguous byte range
-// copied into shared memory with aligned 16-byte loads, and each warp then
-// decodes its blocks out of shared memory.
-template <typename T, int E>
-__global__ void __launch_bounds__(kDecThreads) k_blocked_decode(const uint8_t* __restrict__ s, unsigned long long len,
-                                                                const BlockedHdr* hp,
-                                                                const unsigned long long* __restrict__ P,
-                                                                const uint32_t* __restrict__ RW, T* out,
-                                                                int native_medians, int* err) {
-    using TL = DecTile<T, E>;
-    constexpr int TBD = TL::kBlocks;
-    __shared__ __align__(16) uint8_t stage[TL::kStage];
-    __shared__ unsigned long long s_p[TBD + 1];
-    __shared__ uint32_t s_rank[TBD];
-    __shared__ uint8_t s_nc[TBD];
-    __shared__ unsigned long long s_rank0, s_pa;
-    __shared__ uint32_t s_nnc;
-    __shared__ int s_bad;
-    const BlockedHdr h = *hp;
+struct DecArgs {
+    const uint8_t* s;
+    unsigned long long len;
+    const BlockedHdr* hdr;
+    const unsigned long long* P;   // payload offsets by non-constant rank, [nnc + 1]
+    const uint32_t* RW;            // non-constant rank at each 32-block state word
+    void* out;
+    int native_medians;
+    int* err;
+};
+
+enum : uint8_t { kBlkConst = 0, kBlkCoded = 1, kBlkNone = 2 };
+
+template <typename T, int G>
+__global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
+    using TL = DecTileV<T, G>;
+    constexpr int TB = TL::kBlocks;
+    constexpr int NS = kDecStages;
+    extern __shared__ __align__(128) uint8_t dsm[];
+    __shared__ unsigned long long full[NS], empty[NS];
+    __shared__ uint32_t s_info[NS][TB];    // coded: payload position in the stage; constant: median bits
+    __shared__ uint8_t s_kind[NS][TB];
+    __shared__ uint8_t s_ok[NS];
+    __shared__ uint16_t s_rank[TB];        // producer scratch: rank within the tile
+    const BlockedHdr h = *a.hdr;
     if (!h.ok) return;
+    if (h.bs > (unsigned long long)TL::kBsMax) {
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicExch(a.err, kErrStream);
+        return;
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned long long ntiles = (h.nb + TBD - 1) / TBD;
-    const uint8_t* send = s + len;
-    for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const unsigned long long b0 = tile * TBD;
-        // state bits and ranks within the tile (TBD <= 64: two warps)
-        if (threadIdx.x < 64) {   // whole warps 0 and 1
-            const bool in = threadIdx.x < TBD;
-            const unsigned long long b = b0 + threadIdx.x;
-            const uint32_t bit = (in && b < h.nb) ? (s[h.s_off + (b >> 3)] >> (7 - (b & 7))) & 1u : 0u;
-            const unsigned m = __ballot_sync(0xffffffffu, bit);
-            if (in) {
-                s_nc[threadIdx.x] = (uint8_t)bit;
-                s_rank[threadIdx.x] = __popc(m & ((1u << lane) - 1));   // rank within its warp; fixed below
-            }
-            if (lane == 31) s_p[warp] = __popc(m);                     // warp totals (scratch use of s_p)
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NS; i++) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], kDecWarps);
         }
-        if (threadIdx.x == 0) {
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const unsigned long long nb = h.nb;
+    const long long ntiles = (long long)((nb + TB - 1) / TB);
+    const int bs = (int)h.bs;
+
+    if (warp == kDecWarps) {
+        // ---------------------------------------------------------- producer
+        long long i = 0;
+        for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+            const int slot = (int)(i % NS);
+            if (i >= NS && !mbar_wait(&empty[slot], (uint32_t)((i / NS - 1) & 1))) {
+                if (lane == 0) atomicExch(a.err, kErrLookback);
+                break;
+            }
+            uint8_t* stage = dsm + slot * TL::kStage;
+            const unsigned long long b0 = (unsigned long long)t * TB;
+            const unsigned long long rest = nb - b0;
+            const int nblk = rest < (unsigned long long)TB ? (int)rest : TB;
+            // rank of the tile's first block
             const unsigned long long w = b0 >> 5;
+            const int bit0 = (int)(b0 & 31);
             uint32_t word = 0;
-            for (int j = 0; j < 4; j++) {
-                unsigned long long bi = 4 * w + j;
-                word = (word << 8) | (bi < h.sb ? (uint32_t)s[h.s_off + bi] : 0u);
-            }
-            const int bit = (int)(b0 & 31);
-            s_rank0 = RW[w] + (bit ? __popc(word >> (32 - bit)) : 0);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t tot = (uint32_t)s_p[0] + (TBD > 32 ? (uint32_t)s_p[1] : 0u);
-            s_nnc = tot;
-        }
-        if (TBD > 32 && threadIdx.x >= 32 && threadIdx.x < TBD) s_rank[threadIdx.x] += (uint32_t)s_p[0];
-        __syncthreads();
-        const uint32_t nnc_t = s_nnc;
-        const unsigned long long r0 = s_rank0;
-        if (threadIdx.x <= nnc_t && nnc_t > 0) s_p[threadIdx.x] = P[r0 + threadIdx.x];
-        if (threadIdx.x == 0) s_bad = 0;
-        __syncthreads();
-        if (nnc_t > 0) {
-            const unsigned long long pa = s_p[0], pb = s_p[nnc_t];
-            if (threadIdx.x == 0) {
-                s_pa = pa;
-                if (pb < pa || pb - pa + 32 > (unsigned long long)TL::kStage || h.q_off + pb > len) {
-                    s_bad = 1;
-                    atomicExch(err, kErrStream);
-                }
-            }
-            __syncthreads();
-            if (!s_bad) {
-                // the tile's payloads: one contiguous range, staged at its own 16-byte phase
-                const uint8_t* src = s + h.q_off + pa;
-                const uint32_t sh = (uint32_t)((uintptr_t)src & 15);
-                const uint8_t* gbase = src - sh;
-                const uint32_t nch = (uint32_t)((sh + (pb - pa) + 15) >> 4);
-                for (uint32_t c = threadIdx.x; c < nch; c += kDecThreads) {
-                    const uint8_t* lo = gbase + (c << 4);
-                    if (lo >= s && lo + 16 <= send) *(uint4*)(stage + (c << 4)) = __ldg((const uint4*)lo);
-                    else
-                        for (int j = 0; j < 16; j++) stage[(c << 4) + j] = (lo + j >= s && lo + j < send) ? lo[j] : 0;
-                }
-            }
-        }
-        __syncthreads();
-        const bool bad = nnc_t > 0 && s_bad;
-        for (int k = warp; k < TBD; k += kDecThreads / 32) {
-            const unsigned long long b = b0 + k;
-            if (b >= h.nb) break;
-            const unsigned long long off = b * h.bs;
-            const unsigned long long rem = h.n - off;
-            const int blen = rem < h.bs ? (int)rem : (int)h.bs;
-            T* ob = out + off;
-            if (!s_nc[k]) {
-                const unsigned long long rank = r0 + s_rank[k];
-                const uint8_t* mp = s + h.m_off + 4 * (b - rank);
-                uint32_t mbits = native_medians
-                                     ? ((uint32_t)mp[0] | ((uint32_t)mp[1] << 8) | ((uint32_t)mp[2] << 16) | ((uint32_t)mp[3] << 24))
-                                     : (((uint32_t)mp[0] << 24) | ((uint32_t)mp[1] << 16) | ((uint32_t)mp[2] << 8) | mp[3]);
-                const T m = widen_median<T>(__uint_as_float(mbits));
-                int nv = blen - lane * E;
-                nv = nv < 0 ? 0 : (nv > E ? E : nv);
-                T v[E];
 #pragma unroll
-                for (int e = 0; e < E; e++) v[e] = m;
-                store_lane<T, E>(ob + lane * E, nv, lane_vec_ok<T, E>(ob), v);
-                continue;
+            for (int j = 0; j < 4; j++) {
+                const unsigned long long bi = 4 * w + j;
+                word = (word << 8) | (bi < h.sb ? (uint32_t)a.s[h.s_off + bi] : 0u);
             }
-            if (bad) continue;
-            const uint32_t r = s_rank[k];
-            const unsigned long long pofs = s_p[r] - s_pa, size = s_p[r + 1] - s_p[r];
-            const uint32_t minsz = 5 + (uint32_t)((blen + 3) / 4);
-            if (size < minsz || size > (unsigned long long)TL::kMaxPay) {
-                if (lane == 0) atomicExch(err, kErrStream);
-                continue;
+            const unsigned long long rank0 = a.RW[w] + (bit0 ? __popc(word >> (32 - bit0)) : 0);
+            // state of every block; medians of the constant ones
+            uint32_t ok = 1, running = 0;
+            for (int j = 0; j < TB; j += 32) {
+                const int lb = j + lane;
+                const unsigned long long b = b0 + lb;
+                const bool in = lb < nblk;
+                const uint32_t coded = in ? (a.s[h.s_off + (b >> 3)] >> (7 - (b & 7))) & 1u : 0u;
+                const unsigned m = __ballot_sync(0xffffffffu, coded);
+                const uint32_t r = running + __popc(m & ((1u << lane) - 1));
+                running += __popc(m);
+                if (lb < TB) {
+                    if (!in) {
+                        s_kind[slot][lb] = kBlkNone;
+                    } else if (coded) {
+                        s_kind[slot][lb] = kBlkCoded;
+                        s_rank[lb] = (uint16_t)r;
+                    } else {
+                        const unsigned long long mo = h.m_off + 4 * (b - (rank0 + r));
+                        uint32_t mbits = 0;
+                        if (b >= rank0 + r && mo + 4 <= h.q_off) {
+                            const uint8_t* mp = a.s + mo;
+                            mbits = a.native_medians
+                                        ? ((uint32_t)mp[0] | ((uint32_t)mp[1] << 8) | ((uint32_t)mp[2] << 16) |
+                                           ((uint32_t)mp[3] << 24))
+                                        : (((uint32_t)mp[0] << 24) | ((uint32_t)mp[1] << 16) |
+                                           ((uint32_t)mp[2] << 8) | mp[3]);
+                        } else {
+                            ok = 0;
+                        }
+                        s_info[slot][lb] = mbits;
+                        s_kind[slot][lb] = kBlkConst;
+                    }
+                }
             }
-            const uint32_t sh = (uint32_t)((uintptr_t)(s + h.q_off + s_pa) & 15);
-            dec_block<T, E>(stage + sh + pofs, blen, ob);
+            const uint32_t nnc_t = running;
+            unsigned long long pa = 0, pb = 0;
+            if (rank0 + nnc_t > h.nnc) ok = 0;
+            if (__all_sync(0xffffffffu, ok) && nnc_t) {
+                pa = a.P[rank0];
+                pb = a.P[rank0 + nnc_t];
+                if (pb < pa || pb - pa > (unsigned long long)TB * TL::kMaxPay || h.q_off + pb > a.len) ok = 0;
+            }
+            __syncwarp();
+            const uint8_t* src = a.s + h.q_off + pa;
+            const uint32_t ph = (uint32_t)((uintptr_t)src & 15);
+            if (__all_sync(0xffffffffu, ok) && nnc_t) {
+                for (int j = 0; j < TB; j += 32) {
+                    const int lb = j + lane;
+                    if (lb < nblk && s_kind[slot][lb] == kBlkCoded) {
+                        const unsigned long long k = rank0 + s_rank[lb];
+                        const unsigned long long p0 = a.P[k], p1 = a.P[k + 1];
+                        const unsigned long long rem = h.n - (b0 + lb) * h.bs;
+                        const int blen = rem < h.bs ? (int)rem : bs;
+                        const unsigned long long minsz = 5 + (unsigned long long)((blen + 3) / 4);
+                        if (p0 < pa || p1 > pb || p1 < p0 + minsz || p1 - p0 > (unsigned long long)TL::kMaxPay) ok = 0;
+                        s_info[slot][lb] = ph + (uint32_t)(p0 - pa);
+                    }
+                }
+            }
+            ok = __all_sync(0xffffffffu, ok);
+            // the payload range: aligned interior by TMA, ragged ends by the lanes
+            const unsigned long long nbytes = ok ? pb - pa : 0;
+            const uintptr_t sa = (uintptr_t)src;
+            const uintptr_t a0 = (sa + 15) & ~(uintptr_t)15, a1 = (sa + nbytes) & ~(uintptr_t)15;
+            uint32_t tx = 0;
+            uintptr_t head_end = sa + nbytes, tail_beg = sa + nbytes;
+            if (a1 > a0) {
+                tx = (uint32_t)(a1 - a0);
+                head_end = a0;
+                tail_beg = a1;
+            }
+            for (uintptr_t x = sa + lane; x < head_end; x += 32) stage[ph + (x - sa)] = *(const uint8_t*)x;
+            for (uintptr_t x = tail_beg + lane; x < sa + nbytes; x += 32) stage[ph + (x - sa)] = *(const uint8_t*)x;
+            __threadfence_block();
+            __syncwarp();
+            if (lane == 0) {
+                s_ok[slot] = (uint8_t)ok;
+                if (!ok) atomicExch(a.err, kErrStream);
+                fence_proxy_async();
+                mbar_arrive_expect_tx(&full[slot], tx);
+                if (tx) tma_load_1d(stage + ph + (a0 - sa), (const void*)a0, tx, &full[slot]);
+            }
         }
-        __syncthreads();
+        // copies still in flight finish before the CTA exits
+        for (long long j = i > NS ? i - NS : 0; j < i; j++) mbar_wait(&full[j % NS], (uint32_t)((j / NS) & 1));
+        return;
+    }
+
+    // -------------------------------------------------------------- consumers
+    T* out = (T*)a.out;
+    const bool vec = ((bs * (int)sizeof(T)) & 15) == 0 && ((uintptr_t)out & 15) == 0;
+    const int seg = lane / G;
+    const int lb = warp * TL::kBpw + seg;
+    long long i = 0;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+        const int slot = (int)(i % NS);
+        if (!mbar_wait(&full[slot], (uint32_t)((i / NS) & 1))) {
+            if (lane == 0) atomicExch(a.err, kErrLookback);
+            break;
+        }
+        const unsigned long long b = (unsigned long long)t * TB + lb;
+        const int kind = s_kind[slot][lb];
+        const uint32_t info = s_info[slot][lb];
+        int blen = 0;
+        T* ob = out;
+        if (kind != kBlkNone) {
+            const unsigned long long off = b * h.bs, rem = h.n - off;
+            blen = rem < h.bs ? (int)rem : bs;
+            ob = out + off;
+        }
+        if (kind == kBlkConst) {
+            const T m = widen_median<T>(__uint_as_float(info));
+            T v[EncCfg<T>::E];
+#pragma unroll
+            for (int e = 0; e < EncCfg<T>::E; e++) v[e] = m;
+            store_chunks<T, G>(ob, blen, vec, v);
+        }
+        const bool coded = kind == kBlkCoded && s_ok[slot];
+        const uint8_t* stage = dsm + slot * TL::kStage;
+        dec_segment<T, G>(stage + (coded ? info : 0u), coded ? blen : 0, ob, vec);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
     }
 }
 
-template <typename T, int E>
-static void run_decode(const uint8_t* s, size_t len, size_t nb, const Workspace& ws, void* out, int native,
-                       cudaStream_t st) {
-    const size_t tiles = (nb + DecTile<T, E>::kBlocks - 1) / DecTile<T, E>::kBlocks;
-    const size_t cap = (size_t)sm_count() * 4;
-    int grid = (int)(tiles < cap ? (tiles ? tiles : 1) : cap);
+template <typename T, int G>
+static cudaError_t run_decode(const uint8_t* s, size_t len, size_t nb, const Workspace& ws, void* out, int native,
+                              cudaStream_t st) {
+    using TL = DecTileV<T, G>;
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(k_blocked_decode<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             TL::kDynSmem);
+        if (e != cudaSuccess) return e;
+        attr_set[dev] = true;
+    }
+    const size_t tiles = (nb + TL::kBlocks - 1) / TL::kBlocks;
+    const size_t cap = (size_t)sm_count() * 3;
+    const int grid = (int)(tiles < cap ? (tiles ? tiles : 1) : cap);
+    DecArgs a;
+    a.s = s; a.len = len; a.hdr = ws.bhdr; a.P = ws.p_off; a.RW = ws.rank_w; a.out = out;
+    a.native_medians = native; a.err = ws.err;
     TraceScope tr("blocked_decode", st);
-    k_blocked_decode<T, E><<<grid, kDecThreads, 0, st>>>(s, len, ws.bhdr, ws.p_off, ws.rank_w, (T*)out, native,
-                                                         ws.err);
+    k_blocked_decode<T, G><<<grid, kDecThreadsP, TL::kDynSmem, st>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream, size_t len, size_t n, int bs,
@@ -1248,19 +1340,30 @@ cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream
     // bs comes from the stream header (read by the caller); the device header
     // is validated again by every kernel and a mismatch is reported, not used.
     const int native = layout == kRandomAccessNative;
-    const int E = bs <= 32 ? 1 : bs <= 64 ? 2 : bs <= 128 ? 4 : 8;
     const size_t nb = (n + bs - 1) / bs;
+    // lanes per block as in the encoder: 16 (float) / 8 (double) values per lane
+    const int per = dtype == 0 ? 16 : 8;
+    const int need = (bs + per - 1) / per;
+    const int G = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
     if (dtype == 0) {
-        if (E == 1) run_decode<float, 1>(d_stream, len, nb, ws, d_out, native, s);
-        else if (E == 2) run_decode<float, 2>(d_stream, len, nb, ws, d_out, native, s);
-        else if (E == 4) run_decode<float, 4>(d_stream, len, nb, ws, d_out, native, s);
-        else run_decode<float, 8>(d_stream, len, nb, ws, d_out, native, s);
+        switch (G) {
+            case 1: e = run_decode<float, 1>(d_stream, len, nb, ws, d_out, native, s); break;
+            case 2: e = run_decode<float, 2>(d_stream, len, nb, ws, d_out, native, s); break;
+            case 4: e = run_decode<float, 4>(d_stream, len, nb, ws, d_out, native, s); break;
+            case 8: e = run_decode<float, 8>(d_stream, len, nb, ws, d_out, native, s); break;
+            default: e = run_decode<float, 16>(d_stream, len, nb, ws, d_out, native, s); break;
+        }
     } else {
-        if (E == 1) run_decode<double, 1>(d_stream, len, nb, ws, d_out, native, s);
-        else if (E == 2) run_decode<double, 2>(d_stream, len, nb, ws, d_out, native, s);
-        else if (E == 4) run_decode<double, 4>(d_stream, len, nb, ws, d_out, native, s);
-        else run_decode<double, 8>(d_stream, len, nb, ws, d_out, native, s);
+        switch (G) {
+            case 1: e = run_decode<double, 1>(d_stream, len, nb, ws, d_out, native, s); break;
+            case 2: e = run_decode<double, 2>(d_stream, len, nb, ws, d_out, native, s); break;
+            case 4: e = run_decode<double, 4>(d_stream, len, nb, ws, d_out, native, s); break;
+            case 8: e = run_decode<double, 8>(d_stream, len, nb, ws, d_out, native, s); break;
+            case 16: e = run_decode<double, 16>(d_stream, len, nb, ws, d_out, native, s); break;
+            default: e = run_decode<double, 32>(d_stream, len, nb, ws, d_out, native, s); break;
+        }
     }
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
