@@ -209,23 +209,38 @@ static size_t host_compress(int mode, int dtype, const void* data, size_t n, int
     if (!c->in.ensure(n * es) || !c->out.ensure(cap) || !c->ws.ensure(wsb, true)) { set_err(SZXG_ERR_CUDA); return 0; }
     Workspace ws = ws_carve(c->ws.p, mode, dtype, n, bs);
     cudaStream_t s = c->stream;
+    // a library-allocated output is faulted in by host threads while the GPU works
+    unsigned char* dst = *out;
+    const bool own = dst == nullptr;
+    if (own) {
+        dst = (unsigned char*)malloc(cap ? cap : 1);
+        if (!dst) { set_err(SZXG_ERR_ARG); return 0; }
+        host_prefault_start(dst, cap);
+    }
+    auto drop = [&]() {
+        if (own) {
+            host_prefault_finish(0);
+            free(dst);
+        }
+    };
     cudaError_t e = cudaMemcpyAsync(c->in.p, data, n * es, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) { cuda_fail(e); return 0; }
-    if (enqueue_compress(mode, dtype, c->in.p, n, bs, err_mode, abs_eb, rel, (uint8_t*)c->out.p, c->out.cap, ws, s))
+    if (e != cudaSuccess) { drop(); cuda_fail(e); return 0; }
+    if (enqueue_compress(mode, dtype, c->in.p, n, bs, err_mode, abs_eb, rel, (uint8_t*)c->out.p, c->out.cap, ws, s)) {
+        drop();
         return 0;
+    }
     StreamResult r;
     int err = 0;
     if ((e = cudaMemcpyAsync(&r, ws.result, sizeof(r), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(&err, ws.err, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+        drop();
         cuda_fail(e);
         return 0;
     }
-    if (err) { set_err(err); return 0; }
-    unsigned char* dst = *out;
-    if (!dst) {
-        dst = (unsigned char*)malloc(r.size ? r.size : 1);
-        if (!dst) { set_err(SZXG_ERR_ARG); return 0; }
+    if (err) { drop(); set_err(err); return 0; }
+    if (own) {
+        host_prefault_finish(r.size);
     } else if (out_cap < r.size) {
         set_err(SZXG_ERR_CAPACITY);
         return 0;
@@ -233,9 +248,14 @@ static size_t host_compress(int mode, int dtype, const void* data, size_t n, int
     e = cudaMemcpyAsync(dst, (uint8_t*)c->out.p + r.offset, r.size, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
-        if (!*out) free(dst);
+        if (own) free(dst);
         cuda_fail(e);
         return 0;
+    }
+    if (own) {
+        // give back the tail of the bound-sized allocation
+        unsigned char* shrunk = (unsigned char*)realloc(dst, r.size ? r.size : 1);
+        if (shrunk) dst = shrunk;
     }
     *out = dst;
     set_err(SZXG_OK);
@@ -277,20 +297,31 @@ static void* host_decompress(int mode, int dtype, const unsigned char* bytes, si
     }
     Workspace ws = ws_carve(c->ws.p, mode, dtype, n, bs);
     cudaStream_t s = c->stream;
+    // a library-allocated output is faulted in by host threads while the GPU works
+    const bool own = out == nullptr;
+    void* dst = own ? malloc(n * es) : out;
+    if (!dst) { set_err(SZXG_ERR_ARG); return nullptr; }
+    if (own) host_prefault_start(dst, n * es);
+    auto drop = [&]() {
+        if (own) {
+            host_prefault_finish(0);
+            free(dst);
+        }
+    };
     uint8_t* d_s = (uint8_t*)c->in.p + pad;
     cudaError_t e = cudaMemcpyAsync(d_s, bytes, len, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) { cuda_fail(e); return nullptr; }
-    if (cudaMemsetAsync(ws.err, 0, sizeof(int), s) != cudaSuccess) { set_err(SZXG_ERR_CUDA); return nullptr; }
-    if (enqueue_decompress(mode, dtype, d_s, len, n, bs, c->out.p, ws, s)) return nullptr;
+    if (e != cudaSuccess) { drop(); cuda_fail(e); return nullptr; }
+    if (cudaMemsetAsync(ws.err, 0, sizeof(int), s) != cudaSuccess) { drop(); set_err(SZXG_ERR_CUDA); return nullptr; }
+    if (enqueue_decompress(mode, dtype, d_s, len, n, bs, c->out.p, ws, s)) { drop(); return nullptr; }
     int err = 0;
     if ((e = cudaMemcpyAsync(&err, ws.err, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+        drop();
         cuda_fail(e);
         return nullptr;
     }
-    if (err) { set_err(err); return nullptr; }
-    void* dst = out ? out : malloc(n * es);
-    if (!dst) { set_err(SZXG_ERR_ARG); return nullptr; }
+    if (err) { drop(); set_err(err); return nullptr; }
+    if (own) host_prefault_finish(n * es);
     e = cudaMemcpyAsync(dst, c->out.p, n * es, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {

@@ -93,6 +93,13 @@ constexpr size_t round4(size_t w) { return (w + 3) & ~size_t(3); }
 constexpr size_t enc_status_words(size_t nb) { return round4(nb / 8 + 9); }
 constexpr size_t blocked_status_words(size_t nb) { return enc_status_words(nb) + round4(nb / kAsmBlocksPerTile + 9); }
 
+// Host: fault in the pages of a fresh malloc'd output buffer [p, p+n) on a
+// few worker threads, asynchronously; host_prefault_finish(m) (m <= n) waits
+// until [p, p+m) is resident, skips the rest and ends the job.  One job at a
+// time per process; every start must be paired with a finish.
+void host_prefault_start(void* p, size_t n);
+void host_prefault_finish(size_t m);
+
 size_t ws_bytes(int layout, int dtype, size_t n, int bs);
 Workspace ws_carve(void* base, int layout, int dtype, size_t n, int bs);
 
