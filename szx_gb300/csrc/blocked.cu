@@ -958,8 +958,31 @@ __device__ __forceinline__ void store_chunks(T* ob, int len, bool vec, const T (
     }
 }
 
-template <typename T, int G>
-__device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bool vec) {
+// Lead-byte tables (a lead byte holds 4 codes, MSB first): the four leads as
+// bytes (value 0 in byte 0), and their running minimum from a start of 3
+// (the byte lanes a value still inherits from before its chunk).
+__device__ __forceinline__ void lead_tables_init(uint32_t* lut_ld, uint32_t* lut_cm) {
+    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
+        uint32_t ldb = 0, cmb = 0, m = 3;
+        for (int i = 0; i < 4; i++) {
+            const uint32_t ld = (c >> (6 - 2 * i)) & 3;
+            m = ld < m ? ld : m;
+            ldb |= ld << (8 * i);
+            cmb |= m << (8 * i);
+        }
+        lut_ld[c] = ldb;
+        lut_cm[c] = cmb;
+    }
+}
+__device__ __forceinline__ uint32_t byte_of(uint32_t x, int i) { return __byte_perm(x, 0, 0x4440 | i); }
+// top `n8 / 8` bytes of a 32-bit word set (n8 = 8 * bytes, 0..24)
+__device__ __forceinline__ uint32_t top_bytes_mask(uint32_t n8) { return __funnelshift_r(0u, 0xFFFFFFFFu, n8); }
+
+// FULL: every segment of the warp decodes a whole block of G*E values (no
+// range checks); otherwise values at or past len are ignored.
+template <typename T, int G, bool FULL>
+__device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bool vec, const uint32_t* lut_ld,
+                                            const uint32_t* lut_cm) {
     using C = Chunks<T, G>;
     using EL = Elem<T>;
     using U = typename EL::U;
@@ -974,23 +997,24 @@ __device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bo
     split_reqlen(reqLength, &R, &s);
     R = R < 1 ? 1 : (R > W ? W : R);   // a no-op for valid streams; keeps the shifts defined otherwise
     const int low = 8 * (W - R);
-    const int Lb = (len + 3) / 4;
-    // lead codes (szx/src/szx_TypeManager.cc:198-273: 4 per byte, MSB first) and stored-byte counts
-    uint32_t codes = 0;
+    const int Lb = FULL ? G * NC : (len + 3) / 4;
+    // per chunk: leads, running minima, stored-byte counts and their offsets (bytes of a word)
+    uint32_t ldb[NC], cmb[NC], pre[NC];
     unsigned long long pk = 0;
+    const uint32_t R4 = (uint32_t)R * 0x01010101u;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
         const int c = sl + k * G;
-        const uint32_t code = c < Lb ? (uint32_t)p[5 + c] : 0u;
-        codes |= code << (8 * k);
-        uint32_t n = 0;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int ld = (code >> (6 - 2 * i)) & 3;
-            const int cnt = R - ld;
-            n += (4 * c + i < len && cnt > 0) ? (uint32_t)cnt : 0u;
+        const uint32_t code = (FULL || c < Lb) ? (uint32_t)p[5 + c] : 0u;
+        ldb[k] = lut_ld[code];
+        cmb[k] = lut_cm[code];
+        uint32_t cnt4 = __vsubus4(R4, ldb[k]);   // max(R - lead, 0) per value
+        if constexpr (!FULL) {
+            const int nin = len - 4 * c;
+            cnt4 &= nin >= 4 ? 0xFFFFFFFFu : (nin <= 0 ? 0u : 0xFFFFFFFFu >> (32 - 8 * nin));
         }
-        pk |= (unsigned long long)n << (16 * k);
+        pre[k] = cnt4 * 0x01010100u;   // byte i: bytes of values 0..i-1
+        pk |= (unsigned long long)((cnt4 * 0x01010101u) >> 24) << (16 * k);
     }
     const unsigned long long incl = seg_inclusive_sum<G>(pk);
     const unsigned long long tot = __shfl_sync(0xffffffffu, incl, G - 1, G);
@@ -1002,35 +1026,30 @@ __device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bo
     uint32_t before = ph + 5 + (uint32_t)Lb;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
-        const int c = sl + k * G;
-        uint32_t q = before + (uint32_t)((excl >> (16 * k)) & 0xFFFF);
+        const uint32_t qb = before + (uint32_t)((excl >> (16 * k)) & 0xFFFF);
         before += (uint32_t)((tot >> (16 * k)) & 0xFFFF);
-        const uint32_t code = (codes >> (8 * k)) & 0xFF;
+        const uint32_t ld8 = ldb[k] << 3;
         U run = 0;
-        int mld = 3;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int ld = (code >> (6 - 2 * i)) & 3;
-            const bool in = 4 * c + i < len;
-            const int cnt = (in && R > ld) ? R - ld : 0;
-            const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
-            const uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
-            U raw;
+            const uint32_t q = qb + byte_of(pre[k], i);
+            const uint32_t* wp = buf + (q >> 2);
+            const uint32_t w0 = wp[0], w1 = wp[1];
+            const uint32_t inh = top_bytes_mask(byte_of(ld8, i));   // top lead bytes: from the predecessor
+            // stored bytes land at [W-R, W-lead); the bytes above them are inherited
             if constexpr (sizeof(T) == 4) {
-                raw = lo;
+                const uint32_t sp = __funnelshift_r(w0, w1, q << 3) << low;
+                run = (run & inh) | (sp & ~inh);
             } else {
-                const uint32_t w2 = buf[(q >> 2) + 2];
-                raw = ((unsigned long long)__funnelshift_r(w1, w2, (q & 3) * 8) << 32) | lo;
+                const uint32_t w2 = wp[2];
+                const uint32_t lo = __funnelshift_r(w0, w1, q << 3), hi = __funnelshift_r(w1, w2, q << 3);
+                const unsigned long long sp = (((unsigned long long)hi << 32) | lo) << low;
+                const unsigned long long ih = (unsigned long long)inh << 32;
+                run = (run & ih) | (sp & ~ih);
             }
-            const U inh = ~(~(U)0 >> (8 * ld));          // top ld bytes: inherited
-            // stored bytes land at [W-R, W-ld); everything above is inherited
-            const U sp = (cnt ? (raw << low) : (U)0) & ~inh;
-            run = sp | (run & inh);
             cur[4 * k + i] = run;
-            q += (uint32_t)cnt;
-            if (in && ld < mld) mld = ld;
         }
-        sum[k] = ((uint32_t)mld << 24) | ((uint32_t)(run >> TOPSH) & 0xFFFFFFu);
+        sum[k] = (byte_of(cmb[k], 3) << 24) | ((uint32_t)(run >> TOPSH) & 0xFFFFFFu);
     }
     // last-writer scans: one per chunk round (independent), then the round carries
     uint32_t inc[NC];
@@ -1054,15 +1073,15 @@ __device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bo
         if (sl == 0) ex = kLwNone;
         const uint32_t fin = lw_op(carry_in, ex);
         carry_in = lw_op(carry_in, __shfl_sync(0xffffffffu, inc[k], G - 1, G));
-        const U carry = (U)(fin & 0xFFFFFFu) << TOPSH;
-        const uint32_t code = (codes >> (8 * k)) & 0xFF;
-        int cm = 3;
+        const uint32_t carry = (fin & 0xFFFFFFu) << 8;   // top three bytes of a 32-bit word
+        const uint32_t cm8 = cmb[k] << 3;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int ld = (code >> (6 - 2 * i)) & 3;
-            cm = ld < cm ? ld : cm;
-            const U keep = ~(~(U)0 >> (8 * cm));   // byte lanes inherited from before the chunk
-            const U u = (cur[4 * k + i] | (carry & keep)) << s;
+            const uint32_t keep = top_bytes_mask(byte_of(cm8, i));   // byte lanes inherited from before the chunk
+            U u = cur[4 * k + i];
+            if constexpr (sizeof(T) == 4) u |= carry & keep;
+            else u |= (unsigned long long)(carry & keep) << 32;
+            u <<= s;
             cur[4 * k + i] = u;
             v[4 * k + i] = EL::add(EL::of(u), med);
             bad |= v[4 * k + i] != v[4 * k + i];
@@ -1126,6 +1145,7 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
     __shared__ uint8_t s_kind[NS][TB];
     __shared__ uint8_t s_ok[NS];
     __shared__ uint16_t s_rank[TB];        // producer scratch: rank within the tile
+    __shared__ uint32_t lut_ld[256], lut_cm[256];
     const BlockedHdr h = *a.hdr;
     if (!h.ok) return;
     if (h.bs > (unsigned long long)TL::kBsMax) {
@@ -1140,6 +1160,7 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
         }
         mbar_fence_init();
     }
+    lead_tables_init(lut_ld, lut_cm);
     __syncthreads();
     const unsigned long long nb = h.nb;
     const long long ntiles = (long long)((nb + TB - 1) / TB);
@@ -1287,7 +1308,11 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
         }
         const bool coded = kind == kBlkCoded && s_ok[slot];
         const uint8_t* stage = dsm + slot * TL::kStage;
-        dec_segment<T, G>(stage + (coded ? info : 0u), coded ? blen : 0, ob, vec);
+        // the whole warp takes one path: segments that decode nothing store nothing either way
+        if (__all_sync(0xffffffffu, !coded || blen == TL::kBsMax))
+            dec_segment<T, G, true>(stage + (coded ? info : 0u), coded ? blen : 0, ob, vec, lut_ld, lut_cm);
+        else
+            dec_segment<T, G, false>(stage + (coded ? info : 0u), coded ? blen : 0, ob, vec, lut_ld, lut_cm);
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[slot]);
     }
