@@ -101,76 +101,25 @@ __device__ __forceinline__ void load_chunks(const T* xs, int len, bool vec, T (&
     }
 }
 
-// Segment-wide min/max with the reference's sequential semantics
-// (szx/src/szx_float.cc:322-345): the first value reaching an extreme wins,
-// NaNs are skipped unless the block's first value is NaN.
-template <typename T, int G>
-__device__ __forceinline__ void seg_minmax(const T (&v)[EncCfg<T>::E], int len, T& mn, T& mx) {
-    using C = Chunks<T, G>;
-    constexpr int E = C::E;
-    const int sl = (int)(lane_id() & (G - 1));
-    if constexpr (sizeof(T) == 4) {
-        float lo = __builtin_huge_valf(), hi = -__builtin_huge_valf();
-#pragma unroll
-        for (int e = 0; e < E; e++)
-            if (C::first(sl, e / 4) + (e & 3) < len) { lo = fminf(lo, v[e]); hi = fmaxf(hi, v[e]); }
-#pragma unroll
-        for (int d = G / 2; d > 0; d >>= 1) {
-            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, d, G));
-            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, d, G));
-        }
-        mn = lo;
-        mx = hi;
-    } else {
-        long long lo = 0x7FFFFFFFFFFFFFFFll, hi = (long long)0x8000000000000000ull;
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            unsigned long long u = (unsigned long long)__double_as_longlong(v[e]);
-            bool ok = C::first(sl, e / 4) + (e & 3) < len && (u & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
-            long long k = (long long)(u ^ ((unsigned long long)((long long)u >> 63) & 0x7FFFFFFFFFFFFFFFull));
-            if (ok) { lo = k < lo ? k : lo; hi = k > hi ? k : hi; }
-        }
-#pragma unroll
-        for (int d = G / 2; d > 0; d >>= 1) {
-            long long a = __shfl_xor_sync(0xffffffffu, lo, d, G), b = __shfl_xor_sync(0xffffffffu, hi, d, G);
-            lo = a < lo ? a : lo;
-            hi = b > hi ? b : hi;
-        }
-        auto inv = [](long long k) {
-            unsigned long long u = (unsigned long long)k;
-            return __longlong_as_double((long long)(u ^ ((unsigned long long)(k >> 63) & 0x7FFFFFFFFFFFFFFFull)));
-        };
-        mn = inv(lo);
-        mx = inv(hi);
-    }
-    // a zero extreme takes the sign of the block's first zero; only warps
-    // that met one pay for the search
-    if (__any_sync(0xffffffffu, mn == (T)0 || mx == (T)0)) {
-        int zi = 1 << 30;
-        T zv = 0;
-#pragma unroll
-        for (int e = E - 1; e >= 0; e--) {
-            const int idx = C::first(sl, e / 4) + (e & 3);
-            if (idx < len && v[e] == (T)0 && idx < zi) { zi = idx; zv = v[e]; }
-        }
-        int best = zi;
-#pragma unroll
-        for (int d = G / 2; d > 0; d >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, d, G));
-        const unsigned m = __ballot_sync(0xffffffffu, zi == best && zi < (1 << 30));
-        const unsigned seg0 = lane_id() & ~(unsigned)(G - 1);
-        const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
-        const unsigned mm = m & segmask;
-        const T first = __shfl_sync(0xffffffffu, zv, mm ? __ffs(mm) - 1 : (int)seg0);
-        if (mm) {
-            if (mn == (T)0) mn = first;
-            if (mx == (T)0) mx = first;
-        }
-    }
-    const T x0 = __shfl_sync(0xffffffffu, v[0], 0, G);
-    if (isnan(x0)) { mn = x0; mx = x0; }
-}
-
 // ------------------------------------------------------------------ encode
+//
+// Per-block state a segment keeps in registers from its statistics pass to
+// its emission (szx/src/szx_float.cc:49-252 for one block).
+template <typename T>
+struct BlockEnc {
+    using U = typename Elem<T>::U;
+    static constexpr int E = EncCfg<T>::E;
+    static constexpr int NC = E / 4;
+    U cur[E];                        // shifted words
+    uint32_t cnt4[NC];               // stored bytes of the chunk's 4 values (byte i: value i)
+    uint32_t pre4[NC];               // exclusive offsets of those bytes within the chunk
+    uint32_t codes;                  // lead byte of chunk round k in byte k
+    unsigned long long excl, tot;    // per round (16-bit fields): bytes of earlier lanes, round total
+    int state;                       // 0 constant, 1 coded, 2 no block
+    int reqLength;
+    uint32_t med_bits;               // median as stored (payload or constant list)
+    uint32_t size;                   // payload bytes of a coded block
+};
 
 struct EncArgs {
     unsigned long long* st64;    // tile status, [ntiles + 4]
@@ -190,70 +139,329 @@ struct EncArgs {
     Totals* tot;
 };
 
-template <typename T, int G>
-struct EncTile {
-    static constexpr int E = EncCfg<T>::E;
-    static constexpr int kBsMax = G * E;                               // largest block of this variant
-    static constexpr int kBpw = 32 / G;                                // blocks per warp step
-    static constexpr int kRaw = 16384 / (kBsMax * (int)sizeof(T));
-    static constexpr int kBlocks = kRaw >= 64 ? 64 : (kRaw < 8 ? 8 : kRaw);   // blocks per tile
-    static constexpr int kIn = kBlocks * kBsMax * (int)sizeof(T);      // input bytes per stage
-    static constexpr int kMaxPay = 5 + (kBsMax + 3) / 4 + (int)sizeof(T) * kBsMax;
-    static constexpr int kStage = ((kBlocks * kMaxPay + 32 + 15) / 16) * 16;
-    static constexpr int kDynSmem = 3 * kIn + kStage;
-    static constexpr int kSlots = kBlocks * G;                         // (block, lane) slots per tile
-};
+__device__ __forceinline__ float fmax_nan(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+// bytes [0, n) of a word set (n <= 0: none, n >= 4: all)
+__device__ __forceinline__ uint32_t low_bytes_mask(int n) {
+    return n >= 4 ? 0xFFFFFFFFu : (n <= 0 ? 0u : 0xFFFFFFFFu >> (32 - 8 * n));
+}
 
-// Copy [sh, sh+n) of a 16-aligned shared buffer to global dst (dst % 16 ==
-// sh) with the whole CTA: aligned 16-byte stores, byte stores at the ragged ends.
-__device__ __forceinline__ void cta_copy_out(const uint8_t* stage, uint32_t sh, uint32_t n, uint8_t* dst) {
+// Segment-wide min/max with the reference's sequential semantics
+// (szx/src/szx_float.cc:322-345): the first value reaching an extreme wins,
+// NaNs are skipped unless the block's first value is NaN.  `special` is set
+// (segment-uniform) when the block holds a NaN or an infinity, where the
+// x86 NaN rules of the subtraction matter.
+template <typename T, int G, bool FULL>
+__device__ __forceinline__ void seg_minmax(const T (&v)[EncCfg<T>::E], int len, T& mn, T& mx, bool& special) {
+    using C = Chunks<T, G>;
+    constexpr int E = C::E;
+    const int sl = (int)(lane_id() & (G - 1));
+    if constexpr (sizeof(T) == 4) {
+        float lo = __builtin_huge_valf(), hi = -__builtin_huge_valf(), hn = -__builtin_huge_valf();
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            if (FULL || C::first(sl, e / 4) + (e & 3) < len) {
+                lo = fminf(lo, v[e]);
+                hi = fmaxf(hi, v[e]);
+                hn = fmax_nan(hn, v[e]);
+            }
+        }
+#pragma unroll
+        for (int d = G / 2; d > 0; d >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, d, G));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, d, G));
+            hn = fmax_nan(hn, __shfl_xor_sync(0xffffffffu, hn, d, G));
+        }
+        mn = lo;
+        mx = hi;
+        special = isnan(hn) || isinf(lo) || isinf(hi);
+    } else {
+        long long lo = 0x7FFFFFFFFFFFFFFFll, hi = (long long)0x8000000000000000ull;
+        bool nan = false;
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const unsigned long long u = (unsigned long long)__double_as_longlong(v[e]);
+            const bool in = FULL || C::first(sl, e / 4) + (e & 3) < len;
+            const bool fin = (u & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
+            const long long k = (long long)(u ^ ((unsigned long long)((long long)u >> 63) & 0x7FFFFFFFFFFFFFFFull));
+            if (in && fin) {
+                lo = k < lo ? k : lo;
+                hi = k > hi ? k : hi;
+            }
+            nan |= in && !fin;
+        }
+#pragma unroll
+        for (int d = G / 2; d > 0; d >>= 1) {
+            const long long a = __shfl_xor_sync(0xffffffffu, lo, d, G), b = __shfl_xor_sync(0xffffffffu, hi, d, G);
+            lo = a < lo ? a : lo;
+            hi = b > hi ? b : hi;
+        }
+        auto inv = [](long long k) {
+            const unsigned long long u = (unsigned long long)k;
+            return __longlong_as_double((long long)(u ^ ((unsigned long long)(k >> 63) & 0x7FFFFFFFFFFFFFFFull)));
+        };
+        mn = inv(lo);
+        mx = inv(hi);
+        const unsigned nm = __ballot_sync(0xffffffffu, nan);
+        const unsigned seg0 = lane_id() & ~(unsigned)(G - 1);
+        const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
+        special = (nm & segmask) != 0 || isinf(mn) || isinf(mx);
+    }
+    // a zero extreme takes the sign of the block's first zero; only warps
+    // that met one pay for the search
+    if (__any_sync(0xffffffffu, mn == (T)0 || mx == (T)0)) {
+        int zi = 1 << 30;
+        T zv = 0;
+#pragma unroll
+        for (int e = E - 1; e >= 0; e--) {
+            const int idx = C::first(sl, e / 4) + (e & 3);
+            if ((FULL || idx < len) && v[e] == (T)0 && idx < zi) { zi = idx; zv = v[e]; }
+        }
+        int best = zi;
+#pragma unroll
+        for (int d = G / 2; d > 0; d >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, d, G));
+        const unsigned m = __ballot_sync(0xffffffffu, zi == best && zi < (1 << 30));
+        const unsigned seg0 = lane_id() & ~(unsigned)(G - 1);
+        const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
+        const unsigned mm = m & segmask;
+        const T first = __shfl_sync(0xffffffffu, zv, mm ? __ffs(mm) - 1 : (int)seg0);
+        if (mm) {
+            if (mn == (T)0) mn = first;
+            if (mx == (T)0) mx = first;
+        }
+    }
+    const T x0 = __shfl_sync(0xffffffffu, v[0], 0, G);
+    if (isnan(x0)) { mn = x0; mx = x0; }
+}
+
+// Statistics pass of one block by a G-lane segment: state, reqLength and
+// median (szx/src/szx_float.cc:314-371), the shifted words, lead codes
+// (szx/src/szx_float.cc:94-113) and stored-byte counts, all kept in registers.
+template <typename T, int G, bool FULL>
+__device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, float eb, int omp_stats,
+                                                BlockEnc<T>& b) {
+    using C = Chunks<T, G>;
+    using EL = Elem<T>;
+    using U = typename EL::U;
+    constexpr int E = C::E;
+    constexpr int NC = C::NC;
+    const int sl = (int)(lane_id() & (G - 1));
+    T v[E];
+    load_chunks<T, G>(xs, FULL ? G * E : len, vec, v);
+    T mn, mx;
+    bool special;
+    seg_minmax<T, G, FULL>(v, len, mn, mx, special);
+    int state;
+    float radius_f, median_f;
+    if constexpr (sizeof(T) == 4) {
+        const float range = xsub(mx, mn);
+        radius_f = xdiv(range, 2.0f);
+        median_f = xadd(mn, radius_f);
+        state = (radius_f <= eb) ? 0 : 1;
+    } else if (!omp_stats) {
+        // szx/src/szx_double.cc:991-1003: double statistics, float median/radius
+        const double range = xsub(mx, mn);
+        const double radius = xdiv(range, 2.0);
+        const double median = xadd(mn, radius);
+        state = (radius <= (double)eb) ? 0 : 1;
+        radius_f = xd2f(radius);
+        median_f = xd2f(median);
+    } else {
+        // computeStateMedianRadius_double2 (szx/src/szx_double.cc:1120-1135)
+        const double range = xsub(mx, mn);
+        radius_f = xd2f(xdiv(range, 2.0));
+        median_f = xd2f(xadd(mn, xf2d(radius_f)));
+        state = (radius_f <= eb) ? 0 : 1;
+    }
+    bool zm;
+    const int reqLength = req_length<T>(eb, radius_f, &zm);
+    int R, s;
+    split_reqlen(reqLength, &R, &s);
+    const uint32_t payload_med = zm ? 0u : __float_as_uint(median_f);
+    T med;
+    if constexpr (sizeof(T) == 4) med = __uint_as_float(payload_med);
+    else med = xf2d(median_f);
+    // shifted words (szx/src/szx_float.cc:88-92); x86 NaN rules only where a NaN can arise
+    if (__any_sync(0xffffffffu, special)) {
+#pragma unroll
+        for (int e = 0; e < E; e++) b.cur[e] = EL::bits(xsub(v[e], med)) >> s;
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; e++) b.cur[e] = EL::bits(EL::sub(v[e], med)) >> s;
+    }
+    // lead codes: leading identical bytes with the previous value, capped at 3
+    const uint32_t R4 = (uint32_t)R * 0x01010101u;
+    unsigned long long pk = 0;
+    uint32_t codes = 0;
+    U last_prev = 0;
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+        // value before this chunk: the previous lane's chunk k, or for lane 0
+        // the last lane's chunk k-1 (zero before the block)
+        const U up = __shfl_up_sync(0xffffffffu, b.cur[4 * k + 3], 1, G);
+        const U wrap = __shfl_sync(0xffffffffu, last_prev, G - 1, G);
+        const U prev = sl ? up : (k ? wrap : (U)0);
+        last_prev = b.cur[4 * k + 3];
+        uint32_t ldb = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const U xr = b.cur[4 * k + i] ^ (i ? b.cur[4 * k + i - 1] : prev);
+            uint32_t lz;
+            if constexpr (sizeof(T) == 4) lz = (uint32_t)__clz(xr | 0xFFu) >> 3;
+            else lz = (uint32_t)__clzll((long long)(xr | 0xFFFFFFFFFFull)) >> 3;
+            ldb |= lz << (8 * i);
+        }
+        uint32_t cnt4 = __vsubus4(R4, ldb);   // max(R - lead, 0) per value
+        if constexpr (!FULL) {
+            const uint32_t m = low_bytes_mask(len - 4 * (sl + k * G));
+            ldb &= m;
+            cnt4 &= m;
+        }
+        b.cnt4[k] = cnt4;
+        b.pre4[k] = cnt4 * 0x01010100u;
+        pk |= (unsigned long long)((cnt4 * 0x01010101u) >> 24) << (16 * k);
+        codes |= ((ldb * 0x40100401u) >> 24) << (8 * k);   // 4 leads -> one byte, MSB first
+    }
+    const unsigned long long incl = seg_inclusive_sum<G>(pk);
+    b.tot = __shfl_sync(0xffffffffu, incl, G - 1, G);
+    b.excl = incl - pk;
+    b.codes = codes;
+    uint32_t mid = 0;
+#pragma unroll
+    for (int k = 0; k < NC; k++) mid += (uint32_t)((b.tot >> (16 * k)) & 0xFFFF);
+    const int Lb = FULL ? G * NC : (len + 3) / 4;
+    b.size = 5 + (uint32_t)Lb + mid;
+    b.state = len ? state : 2;
+    b.reqLength = reqLength;
+    b.med_bits = state == 1 ? payload_med : __float_as_uint(median_f);
+}
+
+// Emission of one coded block into the tile's staging buffer (zero-filled):
+// header and lead bytes with byte stores, each value's stored bytes spliced
+// into the staging words with shared-memory atomicOr (a value's bytes span at
+// most two words -- three for double -- which neighbouring values may share).
+template <typename T, int G, bool FULL>
+__device__ __forceinline__ void enc_block_emit(uint8_t* stg, uint32_t loc, int len, const BlockEnc<T>& b) {
+    using C = Chunks<T, G>;
+    using EL = Elem<T>;
+    using U = typename EL::U;
+    constexpr int W = EL::W;
+    constexpr int NC = C::NC;
+    const int sl = (int)(lane_id() & (G - 1));
+    uint8_t* p = stg + loc;
+    if (sl == 0) {
+        p[0] = (uint8_t)b.reqLength;
+        p[1] = (uint8_t)(b.med_bits >> 24);
+        p[2] = (uint8_t)(b.med_bits >> 16);
+        p[3] = (uint8_t)(b.med_bits >> 8);
+        p[4] = (uint8_t)b.med_bits;
+    }
+    const int Lb = FULL ? G * NC : (len + 3) / 4;
+    int R, s;
+    split_reqlen(b.reqLength, &R, &s);
+    (void)s;
+    const int low = 8 * (W - R);
+    uint32_t* sw = (uint32_t*)stg;
+    uint32_t before = loc + 5 + (uint32_t)Lb;
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+        const int c = sl + k * G;
+        // lead codes: 4 per byte, MSB first (szx/src/szx_TypeManager.cc:198-273)
+        if (FULL || c < Lb) p[5 + c] = (uint8_t)(b.codes >> (8 * k));
+        const uint32_t qb = before + (uint32_t)((b.excl >> (16 * k)) & 0xFFFF);
+        before += (uint32_t)((b.tot >> (16 * k)) & 0xFFFF);
+        // mid bytes: bytes [W-R .. W-1-lead] of each shifted word, ascending
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t n = byte_of(b.cnt4[k], i);
+            const uint32_t q = qb + byte_of(b.pre4[k], i);
+            const uint32_t sh = q << 3;             // (q & 3) * 8 once masked by the funnel shifts
+            const uint32_t w = q >> 2, lim = (q & 3) + n;
+            if constexpr (sizeof(T) == 4) {
+                const uint32_t ev = (b.cur[4 * k + i] >> low) & __funnelshift_rc(0xFFFFFFFFu, 0u, 32 - 8 * n);
+                if (n) atomicOr(&sw[w], __funnelshift_l(0u, ev, sh));
+                if (lim > 4) atomicOr(&sw[w + 1], __funnelshift_l(ev, 0u, sh));
+            } else {
+                const unsigned long long m = n >= 8 ? ~0ull : ((1ull << (8 * n)) - 1);
+                const unsigned long long ev = (b.cur[4 * k + i] >> low) & m;
+                const uint32_t lo = (uint32_t)ev, hi = (uint32_t)(ev >> 32);
+                if (n) atomicOr(&sw[w], __funnelshift_l(0u, lo, sh));
+                if (lim > 4) atomicOr(&sw[w + 1], __funnelshift_l(lo, hi, sh));
+                if (lim > 8) atomicOr(&sw[w + 2], __funnelshift_l(hi, 0u, sh));
+            }
+        }
+    }
+}
+
+// Copy n bytes from a 16-aligned staging buffer (data at offset 0) to global
+// dst of any alignment with the whole CTA: 16-byte aligned stores, the
+// staging words realigned with funnel shifts; byte copies at the ragged ends.
+__device__ __forceinline__ void cta_copy_realign(const uint8_t* stg, uint32_t n, uint8_t* dst) {
+    if (n == 0) return;
+    const uint32_t sh = (uint32_t)((uintptr_t)dst & 15);
     uint8_t* gbase = dst - sh;
     const uint32_t end = sh + n, nch = (end + 15) >> 4;
+    const uint32_t* sw = (const uint32_t*)stg;
+    const uint32_t rs = ((16u - sh) & 3u) * 8u;   // byte phase of staging vs. destination words
     for (uint32_t c = threadIdx.x; c < nch; c += blockDim.x) {
         const uint32_t lo = c << 4;
-        if (lo >= sh && lo + 16 <= end) *(uint4*)(gbase + lo) = *(const uint4*)(stage + lo);
+        if (lo >= sh && lo + 16 <= end) {
+            const uint32_t so = lo - sh, w = so >> 2;
+            const uint32_t a0 = sw[w], a1 = sw[w + 1], a2 = sw[w + 2], a3 = sw[w + 3], a4 = sw[w + 4];
+            *(uint4*)(gbase + lo) = make_uint4(__funnelshift_r(a0, a1, rs), __funnelshift_r(a1, a2, rs),
+                                               __funnelshift_r(a2, a3, rs), __funnelshift_r(a3, a4, rs));
+        }
     }
     if (threadIdx.x < 32) {
         const uint32_t last = nch - 1;
         const uint32_t c = threadIdx.x < 16 ? 0 : last;
         const bool part = threadIdx.x < 16 ? (sh > 0 || end < 16) : (last > 0 && (end & 15) != 0);
-        const uint32_t b = (c << 4) + (threadIdx.x & 15);
-        if (part && b >= sh && b < end) gbase[b] = stage[b];
+        const uint32_t gb = (c << 4) + (threadIdx.x & 15);
+        if (part && gb >= sh && gb < end) gbase[gb] = stg[gb - sh];
     }
 }
 
-// One pass over the input, software-pipelined over three tile buffers:
-//   load tile t+2 (TMA bulk copy)  |  pass A of tile t+1, publish its byte count
-//                                  |  resolve tile t's offset, pass B of tile t
-// Pass A (a segment of G lanes per block): statistics, state, reqLength, the
-// shifted words (written back over the input in shared memory), lead codes
-// and stored-byte counts.  Pass B emits the payloads of the whole tile into
-// one staging buffer with byte stores; the CTA then writes the tile's
-// contiguous byte range with aligned 16-byte stores.  Publishing tile t+1's
-// count before resolving tile t means predecessors have normally published
-// long before a tile's look-back walks over them.
+template <typename T, int G>
+struct EncTile {
+    static constexpr int E = EncCfg<T>::E;
+    static constexpr int kBsMax = G * E;                               // largest block of this variant
+    static constexpr int kBpw = 32 / G;                                // blocks per warp
+    static constexpr int kRaw = 16384 / (kBsMax * (int)sizeof(T));
+    static constexpr int kBlocks = kRaw >= 64 ? 64 : (kRaw < 8 ? 8 : kRaw);   // blocks per tile
+    static constexpr int kIn = kBlocks * kBsMax * (int)sizeof(T);      // input bytes per buffer
+    static constexpr int kMaxPay = 5 + (kBsMax + 3) / 4 + (int)sizeof(T) * kBsMax;
+    // payloads of a tile + slack for the word-wise reads of the realigning copy
+    static constexpr int kStage = ((kBlocks * kMaxPay + 32 + 15) / 16) * 16;
+    static constexpr int kDynSmem = 2 * kIn + 2 * kStage;
+    static_assert(kBlocks / kBpw <= kEncWarps, "one block group per warp");
+};
+
+// One pass over the input.  Per tile t_i (double-buffered input by TMA,
+// double-buffered staging):
+//   statistics of every block (registers)  ->  tile scan, publish t_i's byte
+//   count  ->  emission of t_i into zeroed staging  ->  look-back of t_{i-1}
+//   ->  copy-out of t_{i-1} to its place in the payload region.
+// A segment of G lanes owns one block from its statistics to its emission;
+// the look-back of a tile runs one tile later than its publication, so
+// predecessors have normally published by then.
 template <typename T, int G>
 __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     using TL = EncTile<T, G>;
-    using C = Chunks<T, G>;
-    using EL = Elem<T>;
-    using U = typename EL::U;
-    constexpr int W = EL::W;
-    constexpr int E = TL::E;
-    constexpr int NC = C::NC;
     constexpr int TB = TL::kBlocks;
     constexpr int BPW = TL::kBpw;
-    constexpr int NGRP = TB / BPW;   // block groups per tile
+    constexpr int NGRP = TB / BPW;
     extern __shared__ __align__(128) uint8_t dsm[];
-    uint8_t* bufs = dsm;
-    uint8_t* stg = dsm + 3 * TL::kIn;
-    __shared__ unsigned long long bar[3];
+    uint8_t* inb = dsm;
+    uint8_t* stgb = dsm + 2 * TL::kIn;
+    __shared__ unsigned long long bar[2];
     __shared__ uint32_t s_size[2][TB], s_med[2][TB], s_loc[2][TB];
-    __shared__ uint8_t s_state[2][TB], s_req[2][TB];
-    __shared__ uint32_t s_codes[2][TL::kSlots], s_cnt[2][TL::kSlots];
+    __shared__ uint8_t s_state[2][TB];
     __shared__ uint32_t s_agg[2];
+    __shared__ long long s_tile[2];
     __shared__ unsigned long long s_base;
-    __shared__ long long s_next;
     __shared__ int s_skip;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -265,11 +473,13 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     const bool tma_ok = ((uintptr_t)x & 15) == 0;
     const bool vec = ((a.bs * (int)sizeof(T)) & 15) == 0;   // every block starts 16-byte aligned
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 3; i++) mbar_init(&bar[i], 1);
+        for (int i = 0; i < 2; i++) mbar_init(&bar[i], 1);
         mbar_fence_init();
+        s_tile[0] = (long long)atomicAdd(a.tile_ctr, 1ull);
+        s_tile[1] = (long long)atomicAdd(a.tile_ctr, 1ull);
     }
     __syncthreads();
-    uint32_t phase = 0;   // bit i: parity to wait for on buffer i
+    uint32_t phase = 0;   // bit i: parity to wait for on input buffer i
 
     auto tile_count = [&](long long t) {
         const unsigned long long start = (unsigned long long)t * tile_elems;
@@ -280,7 +490,7 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         const unsigned long long cnt = tile_count(t);
         const uint32_t bytes = (uint32_t)(cnt * sizeof(T));
         const uint32_t tbytes = tma_ok ? (bytes & ~15u) : 0u;
-        T* dst = (T*)(bufs + which * TL::kIn);
+        T* dst = (T*)(inb + which * TL::kIn);
         const T* src = x + (unsigned long long)t * tile_elems;
         if (threadIdx.x == 0 && tbytes) {
             fence_proxy_async();
@@ -295,12 +505,6 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
             phase ^= 1u << which;
         }
     };
-    auto acquire = [&]() {
-        __syncthreads();
-        if (threadIdx.x == 0) s_next = (long long)atomicAdd(a.tile_ctr, 1ull);
-        __syncthreads();
-        return s_next;
-    };
     auto block_len = [&](long long t, int lb) {
         const unsigned long long b = (unsigned long long)t * TB + lb;
         if (b >= a.nb) return 0;
@@ -308,140 +512,8 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         return rem < (unsigned long long)a.bs ? (int)rem : a.bs;
     };
 
-    // ---- pass A of tile t (buffer `which`), results in `slot`; warp 0 then
-    // scans the tile and publishes its byte count
-    auto pass_a = [&](long long t, int which, int slot) {
-        T* xt = (T*)(bufs + which * TL::kIn);
-        for (int grp = warp; grp < NGRP; grp += kEncWarps) {
-            const int lb = grp * BPW + seg;
-            const int len = block_len(t, lb);
-            T* xs = xt + (size_t)lb * a.bs;
-            T v[E];
-            load_chunks<T, G>(xs, len, vec, v);
-            T mn, mx;
-            seg_minmax<T, G>(v, len, mn, mx);
-            int state;
-            float radius_f, median_f;
-            if constexpr (sizeof(T) == 4) {
-                float range = xsub(mx, mn);
-                radius_f = xdiv(range, 2.0f);
-                median_f = xadd(mn, radius_f);
-                state = (radius_f <= eb) ? 0 : 1;
-            } else if (!a.omp_stats) {
-                // szx/src/szx_double.cc:991-1003: double statistics, float median/radius
-                double range = xsub(mx, mn);
-                double radius = xdiv(range, 2.0);
-                double median = xadd(mn, radius);
-                state = (radius <= (double)eb) ? 0 : 1;
-                radius_f = xd2f(radius);
-                median_f = xd2f(median);
-            } else {
-                // computeStateMedianRadius_double2 (szx/src/szx_double.cc:1120-1135)
-                double range = xsub(mx, mn);
-                radius_f = xd2f(xdiv(range, 2.0));
-                median_f = xd2f(xadd(mn, xf2d(radius_f)));
-                state = (radius_f <= eb) ? 0 : 1;
-            }
-            bool zm;
-            const int reqLength = req_length<T>(eb, radius_f, &zm);
-            int R, s;
-            split_reqlen(reqLength, &R, &s);
-            const uint32_t med_bits = zm ? 0u : __float_as_uint(median_f);
-            T med;
-            if constexpr (sizeof(T) == 4) med = __uint_as_float(med_bits);
-            else med = xf2d(median_f);
-            // shifted words (szx/src/szx_float.cc:88-92)
-            U cur[E];
-            {
-                T d[E];
-                bool bad = false;
-#pragma unroll
-                for (int e = 0; e < E; e++) {
-                    d[e] = EL::sub(v[e], med);
-                    bad |= d[e] != d[e];
-                }
-                if (__any_sync(0xffffffffu, bad)) {
-#pragma unroll
-                    for (int e = 0; e < E; e++) d[e] = xsub(v[e], med);
-                }
-#pragma unroll
-                for (int e = 0; e < E; e++) cur[e] = EL::bits(d[e]) >> s;
-            }
-            // lead codes and stored-byte counts (szx/src/szx_float.cc:94-113), per chunk
-            uint32_t codes = 0, cnts = 0;
-            U last_prev = 0;
-#pragma unroll
-            for (int k = 0; k < NC; k++) {
-                // value before this chunk: the previous lane's chunk k, or for
-                // lane 0 the last lane's chunk k-1 (zero before the block)
-                const U up = __shfl_up_sync(0xffffffffu, cur[4 * k + 3], 1, G);
-                const U wrap = __shfl_sync(0xffffffffu, last_prev, G - 1, G);
-                U prev = sl ? up : (k ? wrap : (U)0);
-                last_prev = cur[4 * k + 3];
-                const int f = C::first(sl, k);
-                uint32_t byte = 0, nbytes = 0;
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const U xr = cur[4 * k + i] ^ (i ? cur[4 * k + i - 1] : prev);
-                    int lz;
-                    if constexpr (sizeof(T) == 4) lz = __clz(xr | 0xFFu) >> 3;
-                    else lz = __clzll((long long)(xr | 0xFFFFFFFFFFull)) >> 3;
-                    const bool in = f + i < len;
-                    byte = (byte << 2) | (in ? (uint32_t)lz : 0u);
-                    const int c = R - lz;
-                    nbytes += (in && c > 0) ? c : 0;
-                }
-                codes |= byte << (8 * k);
-                cnts |= nbytes << (8 * k);
-            }
-            // keep the shifted words for pass B, over the input values
-            U* cs = (U*)xs;
-#pragma unroll
-            for (int k = 0; k < NC; k++) {
-                const int f = C::first(sl, k);
-                if (vec && f + 4 <= len) {
-                    if constexpr (sizeof(T) == 4) {
-                        *(uint4*)(cs + f) = make_uint4(cur[4 * k], cur[4 * k + 1], cur[4 * k + 2], cur[4 * k + 3]);
-                    } else {
-                        *(ulonglong2*)(cs + f) = make_ulonglong2(cur[4 * k], cur[4 * k + 1]);
-                        *(ulonglong2*)(cs + f + 2) = make_ulonglong2(cur[4 * k + 2], cur[4 * k + 3]);
-                    }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-                        if (f + i < len) cs[f + i] = cur[4 * k + i];
-                }
-            }
-            s_codes[slot][lb * G + sl] = codes;
-            s_cnt[slot][lb * G + sl] = cnts;
-            const uint32_t lane_bytes = (cnts & 0xFF) + ((cnts >> 8) & 0xFF) + ((cnts >> 16) & 0xFF) + (cnts >> 24);
-            const uint32_t size = 5 + (uint32_t)((len + 3) / 4) + seg_sum<G>(lane_bytes);
-            if (sl == 0) {
-                const int st = len ? state : 2;
-                s_state[slot][lb] = (uint8_t)st;
-                s_size[slot][lb] = st == 1 ? size : 0;
-                s_med[slot][lb] = state == 1 ? med_bits : __float_as_uint(median_f);
-                s_req[slot][lb] = (uint8_t)reqLength;
-            }
-        }
-        __syncthreads();
-        if (warp == 0) {
-            const bool in0 = lane < TB, in1 = lane + 32 < TB;
-            const uint32_t sz0 = in0 ? s_size[slot][lane] : 0, sz1 = in1 ? s_size[slot][lane + 32] : 0;
-            const uint32_t i0 = warp_inclusive_sum(sz0);
-            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31);
-            const uint32_t i1 = warp_inclusive_sum(sz1) + t0;
-            const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
-            if (in0) s_loc[slot][lane] = i0 - sz0;
-            if (in1) s_loc[slot][lane + 32] = i1 - sz1;
-            if (lane == 0) s_agg[slot] = agg;
-            prefix_publish(a.st64, t, agg);
-        }
-    };
-
-    // ---- warp 0: offset of tile t, per-block sizes / medians / state bits
+    // warp 0: offset of tile t (slot), its sizes / medians / state bits by block
     auto resolve = [&](long long t, int slot) {
-        if (warp != 0) return;
         const uint32_t agg = s_agg[slot];
         const unsigned long long base = prefix_resolve(a.st64, t, agg, a.err);
         const bool cap_ok = base + agg <= a.payload_cap;
@@ -472,97 +544,78 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         }
     };
 
-    // ---- pass B of tile t: payloads into the staging buffer, then one copy-out
-    auto pass_b = [&](long long t, int which, int slot) {
-        const unsigned long long base = s_base;
-        const uint32_t sh = (uint32_t)((uintptr_t)(a.payload + base) & 15);
-        const T* xt = (const T*)(bufs + which * TL::kIn);
-        for (int grp = warp; grp < NGRP; grp += kEncWarps) {
-            const int lb = grp * BPW + seg;
-            const bool active = s_state[slot][lb] == 1;
-            const int len = block_len(t, lb);
-            const int reqLength = s_req[slot][lb];
-            int R, s;
-            split_reqlen(reqLength, &R, &s);
-            (void)s;
-            const uint32_t codes = s_codes[slot][lb * G + sl];
-            const uint32_t cnts = s_cnt[slot][lb * G + sl];
-            // all chunk offsets from one scan of four packed 16-bit counts
-            unsigned long long pk = 0;
-#pragma unroll
-            for (int k = 0; k < NC; k++) pk |= (unsigned long long)((cnts >> (8 * k)) & 0xFF) << (16 * k);
-            const unsigned long long incl = seg_inclusive_sum<G>(pk);
-            const unsigned long long tot = __shfl_sync(0xffffffffu, incl, G - 1, G);
-            const unsigned long long excl = incl - pk;
-            if (!active) continue;
-            uint8_t* p = stg + sh + s_loc[slot][lb];
-            const int Lb = (len + 3) / 4;
-            if (sl == 0) {
-                const uint32_t mb = s_med[slot][lb];
-                p[0] = (uint8_t)reqLength;
-                p[1] = (uint8_t)(mb >> 24);
-                p[2] = (uint8_t)(mb >> 16);
-                p[3] = (uint8_t)(mb >> 8);
-                p[4] = (uint8_t)mb;
-            }
-            const U* cs = (const U*)(xt + (size_t)lb * a.bs);
-            const int low = 8 * (W - R);
-            uint32_t before = 0;   // bytes of the earlier chunk rounds
-#pragma unroll
-            for (int k = 0; k < NC; k++) {
-                const int f = C::first(sl, k);
-                const int ci = f >> 2;   // chunk index = lead byte index
-                // lead codes: 4 per byte, MSB first (szx/src/szx_TypeManager.cc:198-273)
-                if (ci < Lb) p[5 + ci] = (uint8_t)(codes >> (8 * k));
-                uint8_t* q = p + 5 + Lb + before + (uint32_t)((excl >> (16 * k)) & 0xFFFF);
-                before += (uint32_t)((tot >> (16 * k)) & 0xFFFF);
-                const uint32_t byte = (codes >> (8 * k)) & 0xFF;
-                // mid bytes: bytes [W-R .. W-1-lead] of each shifted word, ascending
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    if (f + i < len) {
-                        const int ld = (byte >> (6 - 2 * i)) & 3;
-                        const int c = R - ld;
-                        const U ev = cs[f + i] >> low;
-#pragma unroll
-                        for (int j = 0; j < W; j++)
-                            if (j < c) q[j] = (uint8_t)(ev >> (8 * j));
-                        q += c > 0 ? c : 0;
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        if (!s_skip) cta_copy_out(stg, sh, s_agg[slot], a.payload + base);
-    };
-
-    // ---- pipeline
-    long long tb = acquire();
-    if (tb < nt) issue(tb, 0);
-    long long ta = acquire();
-    if (ta < nt) issue(ta, 1);
-    int ib = 0, slot = 0;
-    if (tb < nt) {
-        wait_buf(tb, 0);
-        __syncthreads();
-        pass_a(tb, 0, 0);
+    {
+        const long long t0 = s_tile[0], t1 = s_tile[1];
+        if (t0 < nt) issue(t0, 0);
+        if (t1 < nt) issue(t1, 1);
     }
-    while (tb < nt) {
-        const long long tn = acquire();
-        const int in_ = (ib + 2) % 3, ia = (ib + 1) % 3;
-        if (tn < nt) issue(tn, in_);
-        if (ta < nt) {
-            wait_buf(ta, ia);
-            __syncthreads();
-            pass_a(ta, ia, slot ^ 1);
+    long long t_prev = -1;
+    int i = 0;
+    for (;; i++) {
+        const int slot = i & 1;
+        __syncthreads();   // s_tile of this slot, previous copy-out done
+        const long long t = s_tile[slot];
+        if (t >= nt) break;
+        wait_buf(t, slot);
+        // ---- statistics of the tile's blocks, one block per segment
+        const int lb = warp * BPW + seg;
+        const bool mine = warp < NGRP;
+        const int len = mine ? block_len(t, lb) : 0;
+        const bool full = __all_sync(0xffffffffu, len == TL::kBsMax);
+        BlockEnc<T> b;
+        if (mine) {
+            const T* xs = (const T*)(inb + slot * TL::kIn) + (size_t)lb * a.bs;
+            if (full) enc_block_stats<T, G, true>(xs, len, vec, eb, a.omp_stats, b);
+            else enc_block_stats<T, G, false>(xs, len, vec, eb, a.omp_stats, b);
+            if (sl == 0) {
+                s_state[slot][lb] = (uint8_t)b.state;
+                s_size[slot][lb] = b.state == 1 ? b.size : 0;
+                s_med[slot][lb] = b.med_bits;
+            }
         }
-        resolve(tb, slot);
         __syncthreads();
-        pass_b(tb, ib, slot);
-        tb = ta;
-        ta = tn;
-        ib = ia;
-        slot ^= 1;
+        if (warp == 0) {
+            // tile scan and publication of its byte count
+            const bool in0 = lane < TB, in1 = lane + 32 < TB;
+            const uint32_t sz0 = in0 ? s_size[slot][lane] : 0, sz1 = in1 ? s_size[slot][lane + 32] : 0;
+            const uint32_t i0 = warp_inclusive_sum(sz0);
+            const uint32_t c0 = __shfl_sync(0xffffffffu, i0, 31);
+            const uint32_t i1 = warp_inclusive_sum(sz1) + c0;
+            const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
+            if (in0) s_loc[slot][lane] = i0 - sz0;
+            if (in1) s_loc[slot][lane + 32] = i1 - sz1;
+            if (lane == 0) {
+                s_agg[slot] = agg;
+                s_tile[slot] = (long long)atomicAdd(a.tile_ctr, 1ull);   // this buffer's next tile
+            }
+            prefix_publish(a.st64, t, agg);
+        } else {
+            // zero this tile's staging for the spliced emission
+            uint4* z = (uint4*)(stgb + slot * TL::kStage);
+            for (int j = threadIdx.x - 32; j < TL::kStage / 16; j += kEncThreads - 32) z[j] = make_uint4(0, 0, 0, 0);
+        }
+        __syncthreads();
+        {
+            const long long tn = s_tile[slot];
+            if (tn < nt) issue(tn, slot);
+        }
+        if (mine && b.state == 1) {
+            uint8_t* stg = stgb + slot * TL::kStage;
+            if (full) enc_block_emit<T, G, true>(stg, s_loc[slot][lb], len, b);
+            else enc_block_emit<T, G, false>(stg, s_loc[slot][lb], len, b);
+        }
+        if (warp == 0 && t_prev >= 0) resolve(t_prev, slot ^ 1);
+        __syncthreads();
+        if (t_prev >= 0 && !s_skip)
+            cta_copy_realign(stgb + (slot ^ 1) * TL::kStage, s_agg[slot ^ 1], a.payload + s_base);
+        t_prev = t;
+    }
+    // the last tile of this CTA: placed and written out after the loop
+    if (t_prev >= 0) {
+        const int ps = (i & 1) ^ 1;
+        if (warp == 0) resolve(t_prev, ps);
+        __syncthreads();
+        if (!s_skip) cta_copy_realign(stgb + ps * TL::kStage, s_agg[ps], a.payload + s_base);
     }
 }
 
@@ -974,9 +1027,6 @@ __device__ __forceinline__ void lead_tables_init(uint32_t* lut_ld, uint32_t* lut
         lut_cm[c] = cmb;
     }
 }
-__device__ __forceinline__ uint32_t byte_of(uint32_t x, int i) { return __byte_perm(x, 0, 0x4440 | i); }
-// top `n8 / 8` bytes of a 32-bit word set (n8 = 8 * bytes, 0..24)
-__device__ __forceinline__ uint32_t top_bytes_mask(uint32_t n8) { return __funnelshift_r(0u, 0xFFFFFFFFu, n8); }
 
 // FULL: every segment of the warp decodes a whole block of G*E values (no
 // range checks); otherwise values at or past len are ignored.

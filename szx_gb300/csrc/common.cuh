@@ -117,6 +117,10 @@ __device__ __forceinline__ void split_reqlen(int reqLength, int* R, int* s) {
 }
 
 __device__ __forceinline__ uint32_t bswap32(uint32_t v) { return __byte_perm(v, 0, 0x0123); }
+// byte i of x, zero-extended
+__device__ __forceinline__ uint32_t byte_of(uint32_t x, int i) { return __byte_perm(x, 0, 0x4440 | i); }
+// top `n8 / 8` bytes of a 32-bit word set (n8 = 8 * bytes, 0..24)
+__device__ __forceinline__ uint32_t top_bytes_mask(uint32_t n8) { return __funnelshift_r(0u, 0xFFFFFFFFu, n8); }
 
 // ------------------------------------------------------------------ warp scans
 
