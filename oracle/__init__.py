@@ -64,6 +64,13 @@ def lib() -> C.CDLL:
                                               C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
         L.orc_fxr_bound_f32.restype = C.c_float
         L.orc_fxr_bound_f32.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_float, C.c_int]
+        L.orc_fxr_range.restype = C.c_float
+        L.orc_fxr_range.argtypes = [C.c_int, C.c_void_p, C.c_size_t, C.c_int]
+        L.orc_fxr_estimate_cr.restype = C.c_float
+        L.orc_fxr_estimate_cr.argtypes = [C.c_int, C.c_void_p, C.c_size_t, C.c_int, C.c_float,
+                                          C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+        L.orc_fxr_bound.restype = C.c_float
+        L.orc_fxr_bound.argtypes = [C.c_int, C.c_void_p, C.c_size_t, C.c_float, C.c_float, C.c_int]
         _lib = L
     return _lib
 
@@ -155,15 +162,23 @@ def decompress_m3_omp(dtype, stream: np.ndarray, length: int, n: int, threads: i
 
 
 def fxr_bound(x: np.ndarray, ratio: float, tolerance: float, bs: int = 128) -> float:
-    x = np.ascontiguousarray(x, np.float32)
-    return lib().orc_fxr_bound_f32(_ptr(x), x.size, ratio, tolerance, bs)
+    """Error bound the reference fixed-rate search settles on (float or double data)."""
+    x = np.ascontiguousarray(x)
+    return lib().orc_fxr_bound(_dt(x), _ptr(x), x.size, ratio, tolerance, bs)
+
+
+def fxr_range(x: np.ndarray, bs: int = 128) -> float:
+    """Value range over the sampled blocks (every 10th block of bs values)."""
+    x = np.ascontiguousarray(x)
+    return lib().orc_fxr_range(_dt(x), _ptr(x), x.size, bs)
 
 
 def fxr_estimate(x: np.ndarray, eb: float, bs: int = 128):
-    x = np.ascontiguousarray(x, np.float32)
-    a, b = C.c_size_t(), C.c_size_t()
-    cr = lib().orc_fxr_estimate_cr_f32(_ptr(x), x.size, bs, eb, C.byref(a), C.byref(b))
-    return cr, a.value, b.value
+    """(ratio estimate, sum of required bytes, sum of leads, constant sampled blocks)."""
+    x = np.ascontiguousarray(x)
+    a, b, c = C.c_size_t(), C.c_size_t(), C.c_size_t()
+    cr = lib().orc_fxr_estimate_cr(_dt(x), _ptr(x), x.size, bs, eb, C.byref(a), C.byref(b), C.byref(c))
+    return cr, a.value, b.value, c.value
 
 
 # ---------------------------------------------------------------- reference library
@@ -185,6 +200,11 @@ def reference() -> C.CDLL | None:
                                            C.POINTER(C.c_size_t)]
         R.ref_fxr_bound_float.restype = C.c_float
         R.ref_fxr_bound_float.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_float, C.c_int]
+        R.ref_fxr_bound_double.restype = C.c_float
+        R.ref_fxr_bound_double.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_float, C.c_int]
+        R.ref_fxr_estimate.restype = C.c_float
+        R.ref_fxr_estimate.argtypes = [C.c_int, C.c_void_p, C.c_size_t, C.c_int, C.c_float, C.POINTER(C.c_size_t),
+                                       C.POINTER(C.c_size_t), C.POINTER(C.c_float)]
         R.ref_free.restype = None
         R.ref_free.argtypes = [C.c_void_p]
         _ref = R
@@ -225,5 +245,15 @@ def ref_decompress(mode: int, dtype, stream: bytes, n: int) -> np.ndarray:
 
 
 def ref_fxr_bound(x: np.ndarray, ratio: float, tolerance: float, bs: int = 128) -> float:
-    x = np.ascontiguousarray(x, np.float32)
-    return reference().ref_fxr_bound_float(_ptr(x), x.size, ratio, tolerance, bs)
+    x = np.ascontiguousarray(x)
+    R = reference()
+    f = R.ref_fxr_bound_float if x.dtype == np.float32 else R.ref_fxr_bound_double
+    return f(_ptr(x), x.size, ratio, tolerance, bs)
+
+
+def ref_fxr_estimate(x: np.ndarray, eb: float, bs: int = 128):
+    """(ratio estimate, sum of required bytes, sum of leads, sampled range) from the reference."""
+    x = np.ascontiguousarray(x)
+    a, b, r = C.c_size_t(), C.c_size_t(), C.c_float()
+    cr = reference().ref_fxr_estimate(_dt(x), _ptr(x), x.size, bs, eb, C.byref(a), C.byref(b), C.byref(r))
+    return cr, a.value, b.value, r.value

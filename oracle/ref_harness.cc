@@ -46,6 +46,27 @@ float ref_fxr_bound_float(float* data, size_t nbEle, float ratio, float toleranc
     return eb;
 }
 
+// The same search for double data (szx/src/szx_double.cc:918-940).
+float ref_fxr_bound_double(double* data, size_t nbEle, float ratio, float tolerance, int blockSize) {
+    float* radius = NULL; float* median = NULL; double* buffer = NULL;
+    float range = szx::computeRadiusBuffer_double(data, nbEle, 10, blockSize, &radius, &median, &buffer);
+    float eb = szx::estimateErrorBoundbasedonCR_buffered_double(ratio, tolerance, 10, range * 1E-2, blockSize, nbEle,
+                                                                buffer, median, radius);
+    free(radius); free(median); free(buffer);
+    return eb;
+}
+
+// Sampled range and one ratio estimate (szx/src/szx.cc:475-498 C entry points).
+float ref_fxr_estimate(int dataType, void* data, size_t nbEle, int blockSize, float eb, size_t* sumReq,
+                       size_t* sumLead, float* range) {
+    float* radius = NULL; float* median = NULL; void* buffer = NULL;
+    *range = computeRadiusBuffer(data, dataType, nbEle, 10, blockSize, &radius, &median, &buffer);
+    float cr = estimateCRbasedonErrorBound_buffered(dataType, eb, buffer, median, radius, 10, blockSize, nbEle,
+                                                    sumReq, sumLead);
+    free(radius); free(median); free(buffer);
+    return cr;
+}
+
 void ref_free(void* p) { free(p); }
 
 }

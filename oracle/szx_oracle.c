@@ -623,85 +623,142 @@ int orc_decompress_m3_omp(int dt, const uint8_t* s, size_t len, size_t n, void* 
 
 /* ---------------------------------------------------------------- fixed rate */
 
-/* One call of estimateCRbasedonErrorBound_buffered_float (szx/src/szx_float.cc:501-584)
- * over the sampled blocks computeRadiusBuffer_float keeps (every samplingRate-th
- * block, :254-312).  The expression types follow the reference exactly. */
-static float fxr_cr(const float* x, size_t n, int bs, int rate, const float* rads, const float* meds,
-                    float eb, size_t* sumReq, size_t* sumLead) {
+/* Sampled-block statistics of computeRadiusBuffer_float / _double
+ * (szx/src/szx_float.cc:254-312, szx/src/szx_double.cc:437-495): every
+ * rate-th block of bs values (nbEle / (rate*bs) of them), its float radius and
+ * median (double data: computed in double, stored as float), and the sampled
+ * value range (the global extremes start at data[0]). */
+static void fxr_sample_t(int dt, const void* x, size_t n, int bs, int rate, float** rads, float** meds,
+                         float* range) {
+    size_t stride = (size_t)rate * bs, nsamp = n / stride;
+    *rads = (float*)malloc(sizeof(float) * (nsamp + 1));
+    *meds = (float*)malloc(sizeof(float) * (nsamp + 1));
+    if (dt == ORC_FLOAT) {
+        const float* xf = (const float*)x;
+        float gmin = xf[0], gmax = xf[0];
+        for (size_t i = 0; i < nsamp; i++) {
+            const float* d = xf + i * stride;
+            float mn = d[0], mx = d[0];
+            for (int j = 1; j < bs; j++) {
+                float v = d[j];
+                if (mn > v) mn = v;
+                else if (mx < v) mx = v;
+            }
+            if (gmax < mx) gmax = mx;
+            if (gmin > mn) gmin = mn;
+            float r = fdiv32(fsub32(mx, mn), 2);
+            (*rads)[i] = r;
+            (*meds)[i] = fadd32(mn, r);
+        }
+        *range = fsub32(gmax, gmin);
+    } else {
+        const double* xd = (const double*)x;
+        double gmin = xd[0], gmax = xd[0];
+        for (size_t i = 0; i < nsamp; i++) {
+            const double* d = xd + i * stride;
+            double mn = d[0], mx = d[0];
+            for (int j = 1; j < bs; j++) {
+                double v = d[j];
+                if (mn > v) mn = v;
+                else if (mx < v) mx = v;
+            }
+            if (gmax < mx) gmax = mx;
+            if (gmin > mn) gmin = mn;
+            double r = fdiv64(fsub64(mx, mn), 2);
+            (*rads)[i] = d2f(r);
+            (*meds)[i] = d2f(fadd64(mn, r));
+        }
+        *range = d2f(fsub64(gmax, gmin));
+    }
+}
+
+/* One call of estimateCRbasedonErrorBound_buffered_float / _double
+ * (szx/src/szx_float.cc:501-584, szx/src/szx_double.cc:497-580) over the
+ * sampled blocks.  The expression types follow the reference exactly; the
+ * double variant subtracts the (possibly zeroed) float median widened to
+ * double, and its sizes use 65/8 and 8*bs. */
+static float fxr_cr_t(int dt, const void* x, size_t n, int bs, int rate, const float* rads, const float* meds,
+                      float eb, size_t* sumReq, size_t* sumLead, size_t* nconst) {
     size_t nsamp = n / ((size_t)bs * rate);
     size_t ncst = 0;
     *sumLead = 0;
     *sumReq = 0;
     float metadata = 13.0 * bs / n;
-    float block_cost = 33.0 / 8;
+    float block_cost = dt == ORC_FLOAT ? 33.0 / 8 : 65.0 / 8;
     for (size_t i = 0; i < nsamp; i++) {
-        const float* d = x + i * (size_t)bs * rate;
         float median = meds[i], radius = rads[i];
         if (radius <= eb) { ncst++; continue; }
-        int reqLength = reqlen_f32(eb, radius, &median);
+        int reqLength = dt == ORC_FLOAT ? reqlen_f32(eb, radius, &median) : reqlen_f64(eb, radius, &median);
         int R, s;
         split_reqlen(reqLength, &R, &s);
         *sumReq += (size_t)R;
-        uint32_t prev = 0;
         int acc = 0;
-        for (int j = 0; j < bs; j++) {
-            float dv = fsub32(d[j], median);
-            uint32_t cur = f32_bits(dv) >> s;
-            int ld = lead_code32(cur ^ prev);
-            acc += ld >= R ? R : ld;
-            prev = cur;
+        if (dt == ORC_FLOAT) {
+            const float* d = (const float*)x + i * (size_t)bs * rate;
+            uint32_t prev = 0;
+            for (int j = 0; j < bs; j++) {
+                uint32_t cur = f32_bits(fsub32(d[j], median)) >> s;
+                int ld = lead_code32(cur ^ prev);
+                acc += ld >= R ? R : ld;
+                prev = cur;
+            }
+        } else {
+            const double* d = (const double*)x + i * (size_t)bs * rate;
+            uint64_t prev = 0;
+            for (int j = 0; j < bs; j++) {
+                uint64_t cur = f64_bits(fsub64(d[j], f2d(median))) >> s;
+                int ld = lead_code64(cur ^ prev);
+                acc += ld >= R ? R : ld;
+                prev = cur;
+            }
         }
         *sumLead += (size_t)acc;
     }
+    if (nconst) *nconst = ncst;
     float avgReq = 1.0 * (*sumReq) / (nsamp - ncst);
     float avgLead = 1.0 * (*sumLead) / (nsamp - ncst);
     float p_lambda = 1.0 * ncst / nsamp;
-    float cr = 4 * bs / (metadata + block_cost + (1 + (0.25 + avgReq) * bs - avgLead) * (1 - p_lambda));
+    float cr;
+    if (dt == ORC_FLOAT)
+        cr = 4 * bs / (metadata + block_cost + (1 + (0.25 + avgReq) * bs - avgLead) * (1 - p_lambda));
+    else
+        cr = 8 * bs / (metadata + block_cost + (1 + (0.25 + avgReq) * bs - avgLead) * (1 - p_lambda));
     return cr;
 }
 
-static void fxr_sample(const float* x, size_t n, int bs, int rate, float** rads, float** meds, float* range) {
-    size_t stride = (size_t)rate * bs, nsamp = n / stride;
-    *rads = (float*)malloc(sizeof(float) * (nsamp + 1));
-    *meds = (float*)malloc(sizeof(float) * (nsamp + 1));
-    float gmin = x[0], gmax = x[0];
-    for (size_t i = 0; i < nsamp; i++) {
-        const float* d = x + i * stride;
-        float mn = d[0], mx = d[0];
-        for (int j = 1; j < bs; j++) {
-            float v = d[j];
-            if (mn > v) mn = v;
-            else if (mx < v) mx = v;
-        }
-        if (gmax < mx) gmax = mx;
-        if (gmin > mn) gmin = mn;
-        float r = fdiv32(fsub32(mx, mn), 2);
-        (*rads)[i] = r;
-        (*meds)[i] = fadd32(mn, r);
-    }
-    *range = fsub32(gmax, gmin);
+float orc_fxr_range(int dataType, const void* x, size_t n, int bs) {
+    float *rads, *meds, range;
+    fxr_sample_t(dataType, x, n, bs, 10, &rads, &meds, &range);
+    free(rads); free(meds);
+    return range;
 }
 
-float orc_fxr_estimate_cr_f32(const float* x, size_t n, int bs, float eb, size_t* sumReq, size_t* sumLead) {
+float orc_fxr_estimate_cr(int dataType, const void* x, size_t n, int bs, float eb, size_t* sumReq, size_t* sumLead,
+                          size_t* nconst) {
     float *rads, *meds, range;
-    fxr_sample(x, n, bs, 10, &rads, &meds, &range);
-    float cr = fxr_cr(x, n, bs, 10, rads, meds, eb, sumReq, sumLead);
+    fxr_sample_t(dataType, x, n, bs, 10, &rads, &meds, &range);
+    float cr = fxr_cr_t(dataType, x, n, bs, 10, rads, meds, eb, sumReq, sumLead, nconst);
     free(rads); free(meds);
     return cr;
 }
 
-/* estimateErrorBoundbasedonCR_buffered_float, szx/src/szx_float.cc:684-832,
- * started from 1% of the sampled range as szx/src/szx_float.cc:941 does. */
-float orc_fxr_bound_f32(const float* x, size_t n, float target, float tolerance, int bs) {
+float orc_fxr_estimate_cr_f32(const float* x, size_t n, int bs, float eb, size_t* sumReq, size_t* sumLead) {
+    return orc_fxr_estimate_cr(ORC_FLOAT, x, n, bs, eb, sumReq, sumLead, NULL);
+}
+
+/* estimateErrorBoundbasedonCR_buffered_float / _double
+ * (szx/src/szx_float.cc:684-832, szx/src/szx_double.cc:682-830), started from
+ * 1% of the sampled range as szx/src/szx_float.cc:941 does. */
+float orc_fxr_bound(int dataType, const void* x, size_t n, float target, float tolerance, int bs) {
     float *rads, *meds, range;
     const int rate = 10, stride = 8, iters = 10;
-    fxr_sample(x, n, bs, rate, &rads, &meds, &range);
+    fxr_sample_t(dataType, x, n, bs, rate, &rads, &meds, &range);
     float errorBound = range * 1E-2;
     size_t sumReq[20] = {0}, sumLead[20] = {0};
     float bounds[20], ratios[20];
     int k = 0, i, j;
     size_t sr = 0, sl = 0;
-    float CR = fxr_cr(x, n, bs, rate, rads, meds, errorBound, &sr, &sl);
+    float CR = fxr_cr_t(dataType, x, n, bs, rate, rads, meds, errorBound, &sr, &sl, NULL);
     sumReq[k] = sr; sumLead[k] = sl; bounds[k] = errorBound; ratios[k] = CR; k++;
     float result = 0;
     if (fabs(target - CR) < tolerance) { result = errorBound; goto done; }
@@ -712,7 +769,7 @@ float orc_fxr_bound_f32(const float* x, size_t n, float target, float tolerance,
         left = errorBound / stride;
         right = errorBound;
         for (i = 0; i < iters; i++) {
-            CR = fxr_cr(x, n, bs, rate, rads, meds, left, &sr, &sl);
+            CR = fxr_cr_t(dataType, x, n, bs, rate, rads, meds, left, &sr, &sl, NULL);
             sumReq[k] = sr; sumLead[k] = sl; bounds[k] = left; ratios[k] = CR; k++;
             if (fabs(CR - target) < targetTol) { found = 1; result = left; break; }
             if (target > CR) break;
@@ -723,7 +780,7 @@ float orc_fxr_bound_f32(const float* x, size_t n, float target, float tolerance,
         left = errorBound;
         right = errorBound * stride;
         for (i = 0; i < iters; i++) {
-            CR = fxr_cr(x, n, bs, rate, rads, meds, right, &sr, &sl);
+            CR = fxr_cr_t(dataType, x, n, bs, rate, rads, meds, right, &sr, &sl, NULL);
             sumReq[k] = sr; sumLead[k] = sl; bounds[k] = right; ratios[k] = CR; k++;
             if (fabs(target - CR) < targetTol) { found = 1; result = right; break; }
             if (target < CR) break;
@@ -734,7 +791,7 @@ float orc_fxr_bound_f32(const float* x, size_t n, float target, float tolerance,
     if (!found) {
         for (i = 0; i < iters; i++) {
             errorBound = (left + right) / 2;
-            CR = fxr_cr(x, n, bs, rate, rads, meds, errorBound, &sr, &sl);
+            CR = fxr_cr_t(dataType, x, n, bs, rate, rads, meds, errorBound, &sr, &sl, NULL);
             int appeared = 0;
             for (j = 0; j < k; j++)
                 if (sumReq[j] == sr && sumLead[j] == sl) { appeared = 1; break; }
@@ -754,4 +811,8 @@ float orc_fxr_bound_f32(const float* x, size_t n, float target, float tolerance,
 done:
     free(rads); free(meds);
     return result;
+}
+
+float orc_fxr_bound_f32(const float* x, size_t n, float target, float tolerance, int bs) {
+    return orc_fxr_bound(ORC_FLOAT, x, n, target, tolerance, bs);
 }

@@ -73,6 +73,11 @@ int    orc_decompress_m3_omp(int dataType, const uint8_t* stream, size_t len, si
 float orc_fxr_estimate_cr_f32(const float* x, size_t n, int blockSize, float errorBound,
                               size_t* sumReqNbBytes, size_t* sumActualLead);
 float orc_fxr_bound_f32(const float* x, size_t n, float ratio, float tolerance, int blockSize);
+/* The same for either type (szx/src/szx_double.cc:437-495, :497-580, :682-830). */
+float orc_fxr_range(int dataType, const void* x, size_t n, int blockSize);
+float orc_fxr_estimate_cr(int dataType, const void* x, size_t n, int blockSize, float errorBound,
+                          size_t* sumReqNbBytes, size_t* sumActualLead, size_t* nbConstant);
+float orc_fxr_bound(int dataType, const void* x, size_t n, float ratio, float tolerance, int blockSize);
 
 #ifdef __cplusplus
 }

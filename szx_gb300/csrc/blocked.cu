@@ -30,6 +30,7 @@
 //   scan over 4-value chunks.
 #include "common.cuh"
 #include "kernels.h"
+#include "segment.cuh"
 
 namespace szxg {
 
@@ -37,69 +38,6 @@ constexpr int kEncWarps = 8;
 constexpr int kEncThreads = kEncWarps * 32;
 constexpr int kIdxThreads = 256;
 constexpr int kIdxItems = 8;   // items per thread in the index scans
-
-// ------------------------------------------------------------------ segment helpers
-//
-// A block is handled by a segment of G lanes (G a power of two), each lane
-// holding E consecutive values (16 float / 8 double).  Reductions and scans
-// run inside segments with shuffle widths of G, so several blocks share one
-// warp instruction and the per-block work is replicated G times, not 32.
-
-template <typename T> struct EncCfg;
-template <> struct EncCfg<float> { static constexpr int E = 16; };    // values per lane
-template <> struct EncCfg<double> { static constexpr int E = 8; };
-
-template <int G, typename V>
-__device__ __forceinline__ V seg_sum(V v) {
-#pragma unroll
-    for (int d = G / 2; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d, G);
-    return v;
-}
-template <int G, typename V>
-__device__ __forceinline__ V seg_inclusive_sum(V v) {
-    const int sl = (int)(lane_id() & (G - 1));
-#pragma unroll
-    for (int d = 1; d < G; d <<= 1) {
-        V o = __shfl_up_sync(0xffffffffu, v, d, G);
-        if (sl >= d) v += o;
-    }
-    return v;
-}
-
-// Chunked lane layout.  A block is split into chunks of 4 values (one lead
-// byte each); lane sl of a G-lane segment owns chunks sl, sl+G, sl+2G, ...
-// so consecutive lanes touch consecutive chunks (no shared-memory bank
-// conflicts) while each chunk stays contiguous for the XOR chain.
-template <typename T, int G>
-struct Chunks {
-    static constexpr int E = EncCfg<T>::E;
-    static constexpr int NC = E / 4;                  // chunks per lane
-    static constexpr int CB = 4 * (int)sizeof(T);     // bytes per chunk
-    // first value of the lane's k-th chunk
-    static __device__ __forceinline__ int first(int sl, int k) { return 4 * (sl + k * G); }
-};
-
-template <typename T, int G>
-__device__ __forceinline__ void load_chunks(const T* xs, int len, bool vec, T (&v)[EncCfg<T>::E]) {
-    using C = Chunks<T, G>;
-    const int sl = (int)(lane_id() & (G - 1));
-#pragma unroll
-    for (int k = 0; k < C::NC; k++) {
-        const int f = C::first(sl, k);
-        if (vec && f + 4 <= len) {
-            if constexpr (sizeof(T) == 4) {
-                const float4 q = *(const float4*)(xs + f);
-                v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
-            } else {
-                const double2 a = *(const double2*)(xs + f), b = *(const double2*)(xs + f + 2);
-                v[4 * k] = a.x; v[4 * k + 1] = a.y; v[4 * k + 2] = b.x; v[4 * k + 3] = b.y;
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; i++) v[4 * k + i] = f + i < len ? xs[f + i] : (T)0;
-        }
-    }
-}
 
 // ------------------------------------------------------------------ encode
 //
@@ -138,104 +76,6 @@ struct EncArgs {
     int* err;
     Totals* tot;
 };
-
-__device__ __forceinline__ float fmax_nan(float a, float b) {
-    float r;
-    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
-    return r;
-}
-// bytes [0, n) of a word set (n <= 0: none, n >= 4: all)
-__device__ __forceinline__ uint32_t low_bytes_mask(int n) {
-    return n >= 4 ? 0xFFFFFFFFu : (n <= 0 ? 0u : 0xFFFFFFFFu >> (32 - 8 * n));
-}
-
-// Segment-wide min/max with the reference's sequential semantics
-// (szx/src/szx_float.cc:322-345): the first value reaching an extreme wins,
-// NaNs are skipped unless the block's first value is NaN.  `special` is set
-// (segment-uniform) when the block holds a NaN or an infinity, where the
-// x86 NaN rules of the subtraction matter.
-template <typename T, int G, bool FULL>
-__device__ __forceinline__ void seg_minmax(const T (&v)[EncCfg<T>::E], int len, T& mn, T& mx, bool& special) {
-    using C = Chunks<T, G>;
-    constexpr int E = C::E;
-    const int sl = (int)(lane_id() & (G - 1));
-    if constexpr (sizeof(T) == 4) {
-        float lo = __builtin_huge_valf(), hi = -__builtin_huge_valf(), hn = -__builtin_huge_valf();
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            if (FULL || C::first(sl, e / 4) + (e & 3) < len) {
-                lo = fminf(lo, v[e]);
-                hi = fmaxf(hi, v[e]);
-                hn = fmax_nan(hn, v[e]);
-            }
-        }
-#pragma unroll
-        for (int d = G / 2; d > 0; d >>= 1) {
-            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, d, G));
-            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, d, G));
-            hn = fmax_nan(hn, __shfl_xor_sync(0xffffffffu, hn, d, G));
-        }
-        mn = lo;
-        mx = hi;
-        special = isnan(hn) || isinf(lo) || isinf(hi);
-    } else {
-        long long lo = 0x7FFFFFFFFFFFFFFFll, hi = (long long)0x8000000000000000ull;
-        bool nan = false;
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            const unsigned long long u = (unsigned long long)__double_as_longlong(v[e]);
-            const bool in = FULL || C::first(sl, e / 4) + (e & 3) < len;
-            const bool fin = (u & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
-            const long long k = (long long)(u ^ ((unsigned long long)((long long)u >> 63) & 0x7FFFFFFFFFFFFFFFull));
-            if (in && fin) {
-                lo = k < lo ? k : lo;
-                hi = k > hi ? k : hi;
-            }
-            nan |= in && !fin;
-        }
-#pragma unroll
-        for (int d = G / 2; d > 0; d >>= 1) {
-            const long long a = __shfl_xor_sync(0xffffffffu, lo, d, G), b = __shfl_xor_sync(0xffffffffu, hi, d, G);
-            lo = a < lo ? a : lo;
-            hi = b > hi ? b : hi;
-        }
-        auto inv = [](long long k) {
-            const unsigned long long u = (unsigned long long)k;
-            return __longlong_as_double((long long)(u ^ ((unsigned long long)(k >> 63) & 0x7FFFFFFFFFFFFFFFull)));
-        };
-        mn = inv(lo);
-        mx = inv(hi);
-        const unsigned nm = __ballot_sync(0xffffffffu, nan);
-        const unsigned seg0 = lane_id() & ~(unsigned)(G - 1);
-        const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
-        special = (nm & segmask) != 0 || isinf(mn) || isinf(mx);
-    }
-    // a zero extreme takes the sign of the block's first zero; only warps
-    // that met one pay for the search
-    if (__any_sync(0xffffffffu, mn == (T)0 || mx == (T)0)) {
-        int zi = 1 << 30;
-        T zv = 0;
-#pragma unroll
-        for (int e = E - 1; e >= 0; e--) {
-            const int idx = C::first(sl, e / 4) + (e & 3);
-            if ((FULL || idx < len) && v[e] == (T)0 && idx < zi) { zi = idx; zv = v[e]; }
-        }
-        int best = zi;
-#pragma unroll
-        for (int d = G / 2; d > 0; d >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, d, G));
-        const unsigned m = __ballot_sync(0xffffffffu, zi == best && zi < (1 << 30));
-        const unsigned seg0 = lane_id() & ~(unsigned)(G - 1);
-        const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
-        const unsigned mm = m & segmask;
-        const T first = __shfl_sync(0xffffffffu, zv, mm ? __ffs(mm) - 1 : (int)seg0);
-        if (mm) {
-            if (mn == (T)0) mn = first;
-            if (mx == (T)0) mx = first;
-        }
-    }
-    const T x0 = __shfl_sync(0xffffffffu, v[0], 0, G);
-    if (isnan(x0)) { mn = x0; mx = x0; }
-}
 
 // Statistics pass of one block by a G-lane segment: state, reqLength and
 // median (szx/src/szx_float.cc:314-371), the shifted words, lead codes
@@ -293,27 +133,14 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
         for (int e = 0; e < E; e++) b.cur[e] = EL::bits(EL::sub(v[e], med)) >> s;
     }
     // lead codes: leading identical bytes with the previous value, capped at 3
+    uint32_t ldbs[NC];
+    seg_lead_bytes<T, G>(b.cur, ldbs);
     const uint32_t R4 = (uint32_t)R * 0x01010101u;
     unsigned long long pk = 0;
     uint32_t codes = 0;
-    U last_prev = 0;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
-        // value before this chunk: the previous lane's chunk k, or for lane 0
-        // the last lane's chunk k-1 (zero before the block)
-        const U up = __shfl_up_sync(0xffffffffu, b.cur[4 * k + 3], 1, G);
-        const U wrap = __shfl_sync(0xffffffffu, last_prev, G - 1, G);
-        const U prev = sl ? up : (k ? wrap : (U)0);
-        last_prev = b.cur[4 * k + 3];
-        uint32_t ldb = 0;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const U xr = b.cur[4 * k + i] ^ (i ? b.cur[4 * k + i - 1] : prev);
-            uint32_t lz;
-            if constexpr (sizeof(T) == 4) lz = (uint32_t)__clz(xr | 0xFFu) >> 3;
-            else lz = (uint32_t)__clzll((long long)(xr | 0xFFFFFFFFFFull)) >> 3;
-            ldb |= lz << (8 * i);
-        }
+        uint32_t ldb = ldbs[k];
         uint32_t cnt4 = __vsubus4(R4, ldb);   // max(R - lead, 0) per value
         if constexpr (!FULL) {
             const uint32_t m = low_bytes_mask(len - 4 * (sl + k * G));
@@ -512,6 +339,7 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         return rem < (unsigned long long)a.bs ? (int)rem : a.bs;
     };
 
+    unsigned long long nnc_cta = 0;   // warp 0 lane 0: non-constant blocks of this CTA's tiles
     // warp 0: offset of tile t (slot), its sizes / medians / state bits by block
     auto resolve = [&](long long t, int slot) {
         const uint32_t agg = s_agg[slot];
@@ -537,7 +365,7 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
 #pragma unroll
             for (int k = 0; k < TB / 8; k++) sbp[k] = (uint8_t)((k < 4 ? r0 : r1) >> (24 - 8 * (k & 3)));
             if (!cap_ok) atomicExch(a.err, kErrCapacity);
-            atomicAdd(&a.tot->nnc, (unsigned long long)(__popc(m01[0]) + __popc(m01[1])));
+            nnc_cta += (unsigned long long)(__popc(m01[0]) + __popc(m01[1]));
             if (t == nt - 1) a.tot->payload_bytes = base + agg;
             s_base = base;
             s_skip = !cap_ok;
@@ -617,6 +445,7 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         __syncthreads();
         if (!s_skip) cta_copy_realign(stgb + ps * TL::kStage, s_agg[ps], a.payload + s_base);
     }
+    if (threadIdx.x == 0 && nnc_cta) atomicAdd(&a.tot->nnc, nnc_cta);
 }
 
 // Header, size index, state bits and medians (szx/src/szx_float.cc:1437-1483).
@@ -988,28 +817,6 @@ __device__ __forceinline__ uint32_t lw_op(uint32_t a, uint32_t b) {
     return ((ma < mb ? ma : mb) << 24) | (a & 0xFFFFFFu & ~mask) | (b & mask);
 }
 constexpr uint32_t kLwNone = 3u << 24;   // writes nothing; the value before a block is zero
-
-template <typename T, int G>
-__device__ __forceinline__ void store_chunks(T* ob, int len, bool vec, const T (&v)[EncCfg<T>::E]) {
-    using C = Chunks<T, G>;
-    const int sl = (int)(lane_id() & (G - 1));
-#pragma unroll
-    for (int k = 0; k < C::NC; k++) {
-        const int f = C::first(sl, k);
-        if (vec && f + 4 <= len) {
-            if constexpr (sizeof(T) == 4) {
-                *(float4*)(ob + f) = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-            } else {
-                *(double2*)(ob + f) = make_double2(v[4 * k], v[4 * k + 1]);
-                *(double2*)(ob + f + 2) = make_double2(v[4 * k + 2], v[4 * k + 3]);
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-                if (f + i < len) ob[f + i] = v[4 * k + i];
-        }
-    }
-}
 
 // Lead-byte tables (a lead byte holds 4 codes, MSB first): the four leads as
 // bytes (value 0 in byte 0), and their running minimum from a start of 3

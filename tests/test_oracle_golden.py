@@ -147,11 +147,30 @@ def test_oracle_tiny_and_ragged_sizes():
                 assert _violations(x.astype(np.float64), y, 1e-3).size == 0, (dt, n, mode, bs)
 
 
-def test_fxr_estimator_matches_reference_when_built():
-    if O.reference() is None:
-        pytest.skip("reference library not built here (needs the reference sources)")
+def _fxr_fields():
     rng = np.random.default_rng(11)
     i = np.arange(1 << 18)
-    x = (np.sin(i / 300.0) + 0.01 * rng.normal(size=i.size)).astype(np.float32)
-    for ratio in (4.0, 8.0, 16.0):
-        assert O.fxr_bound(x, ratio, 0.05) == O.ref_fxr_bound(x, ratio, 0.05)
+    smooth = np.sin(i / 300.0) + 0.01 * rng.normal(size=i.size)
+    steps = np.repeat(rng.normal(size=i.size // 512), 512) + 1e-4 * rng.normal(size=i.size)
+    walk = np.cumsum(rng.normal(size=i.size)) * 1e-3
+    return {"smooth": smooth, "steps": steps, "walk": walk}
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_fxr_search_matches_reference_when_built(dt):
+    """Sampled range, one ratio estimate and the settled bound of the
+    fixed-rate search equal the reference's, number for number."""
+    if O.reference() is None:
+        pytest.skip("reference library not built here (needs the reference sources)")
+    for name, f in _fxr_fields().items():
+        x = (f * (1e3 if dt == np.float64 else 1.0)).astype(dt)
+        bits = lambda v: np.float32(v).view(np.uint32)   # NaN-safe: an all-constant sample gives 0/0
+        for scale in (1e-5, 1e-3, 3e-2):
+            eb = np.float32(scale * np.ptp(x))
+            cr, req, lead, rng_ = O.ref_fxr_estimate(x, eb)
+            ocr, oreq, olead, _ = O.fxr_estimate(x, eb)
+            assert (bits(ocr), oreq, olead) == (bits(cr), req, lead), (name, scale)
+            assert bits(O.fxr_range(x)) == bits(rng_), name
+        for ratio in (4.0, 8.0, 16.0, 32.0):
+            for tol in (0.05, 0.1):
+                assert bits(O.fxr_bound(x, ratio, tol)) == bits(O.ref_fxr_bound(x, ratio, tol)), (name, ratio, tol)
