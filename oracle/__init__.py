@@ -217,12 +217,13 @@ def _take(R, p: int, nbytes: int) -> bytes:
     return b
 
 
-def ref_compress_args(mode: int, x: np.ndarray, err_mode: int, abs_eb: float, rel: float) -> bytes:
+def ref_compress_args(mode: int, x: np.ndarray, err_mode: int, abs_eb: float, rel: float, ratio: float = 0.0,
+                      tolerance: float = 0.0) -> bytes:
     """SZx_fast_compress_args of the reference (block size 128)."""
     R = reference()
     x = np.ascontiguousarray(x)
     sz = C.c_size_t()
-    p = R.SZx_fast_compress_args(mode, _dt(x), _ptr(x), C.byref(sz), err_mode, abs_eb, rel, 0.0, 0.0,
+    p = R.SZx_fast_compress_args(mode, _dt(x), _ptr(x), C.byref(sz), err_mode, abs_eb, rel, ratio, tolerance,
                                  0, 0, 0, 0, x.size)
     return _take(R, p, sz.value)
 

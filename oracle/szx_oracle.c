@@ -715,9 +715,10 @@ static float fxr_cr_t(int dt, const void* x, size_t n, int bs, int rate, const f
         *sumLead += (size_t)acc;
     }
     if (nconst) *nconst = ncst;
-    float avgReq = 1.0 * (*sumReq) / (nsamp - ncst);
-    float avgLead = 1.0 * (*sumLead) / (nsamp - ncst);
-    float p_lambda = 1.0 * ncst / nsamp;
+    /* 0/0 (every sampled block constant) as x86 computes it, on any host */
+    float avgReq = fdiv64(1.0 * (*sumReq), (double)(nsamp - ncst));
+    float avgLead = fdiv64(1.0 * (*sumLead), (double)(nsamp - ncst));
+    float p_lambda = fdiv64(1.0 * ncst, (double)nsamp);
     float cr;
     if (dt == ORC_FLOAT)
         cr = 4 * bs / (metadata + block_cost + (1 + (0.25 + avgReq) * bs - avgLead) * (1 - p_lambda));

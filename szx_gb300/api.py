@@ -111,6 +111,53 @@ def fast_decompress(fastMode: int, dtype, stream: bytes, n: int | None = None, d
     return np.frombuffer(_take(p, n * nd.itemsize), nd).copy()
 
 
+def estimate_error_bound(data: np.ndarray, compressionRatio: float, tolerance: float, initErrorBound: float,
+                         blockSize: int = 128) -> float:
+    """SZx_estimateErrorBoundbasedonCR: the bound the sampled-ratio search settles on."""
+    x = np.ascontiguousarray(data)
+    eb = lib().SZx_estimateErrorBoundbasedonCR(_dtype_code(x.dtype), compressionRatio, tolerance, x.ctypes.data,
+                                               initErrorBound, blockSize, x.size)
+    if last_error():
+        raise SZxError(last_error(), "SZx_estimateErrorBoundbasedonCR")
+    return eb
+
+
+def compute_radius_buffer(data: np.ndarray, samplingRate: int = 10, blockSize: int = 128):
+    """computeRadiusBuffer: (sampled range, radius[], median[], copies of the sampled blocks)."""
+    x = np.ascontiguousarray(data)
+    rp, mp, bp = C.POINTER(C.c_float)(), C.POINTER(C.c_float)(), C.c_void_p()
+    rng = lib().computeRadiusBuffer(x.ctypes.data, _dtype_code(x.dtype), x.size, samplingRate, blockSize,
+                                    C.byref(rp), C.byref(mp), C.byref(bp))
+    if last_error():
+        raise SZxError(last_error(), "computeRadiusBuffer")
+    ns = x.size // (samplingRate * blockSize)
+    free = libc().free
+    try:
+        rads = np.ctypeslib.as_array(rp, shape=(ns,)).copy() if ns else np.zeros(0, np.float32)
+        meds = np.ctypeslib.as_array(mp, shape=(ns,)).copy() if ns else np.zeros(0, np.float32)
+        buf = (np.frombuffer(C.string_at(bp.value, ns * blockSize * x.itemsize), x.dtype).copy()
+               if ns else np.zeros(0, x.dtype))
+    finally:
+        free(C.cast(rp, C.c_void_p)); free(C.cast(mp, C.c_void_p)); free(bp)
+    return rng, rads, meds, buf
+
+
+def estimate_cr_buffered(buffer: np.ndarray, medians: np.ndarray, radii: np.ndarray, errorBound: float, nbEle: int,
+                         samplingRate: int = 10, blockSize: int = 128):
+    """estimateCRbasedonErrorBound_buffered: (ratio estimate, sum of required bytes, sum of leads)."""
+    b = np.ascontiguousarray(buffer)
+    m = np.ascontiguousarray(medians, np.float32)
+    r = np.ascontiguousarray(radii, np.float32)
+    a, c = C.c_size_t(), C.c_size_t()
+    fp = C.POINTER(C.c_float)
+    cr = lib().estimateCRbasedonErrorBound_buffered(_dtype_code(b.dtype), errorBound, b.ctypes.data,
+                                                    m.ctypes.data_as(fp), r.ctypes.data_as(fp), samplingRate,
+                                                    blockSize, nbEle, C.byref(a), C.byref(c))
+    if last_error():
+        raise SZxError(last_error(), "estimateCRbasedonErrorBound_buffered")
+    return cr, a.value, c.value
+
+
 def compress_blocked(data: np.ndarray, absErrBound: float, blockSize: int, native_medians: bool = False) -> bytes:
     """SZx_fast_compress_args_unpredictable_blocked(_randomaccess_openmp)."""
     x = np.ascontiguousarray(data)

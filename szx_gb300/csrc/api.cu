@@ -131,7 +131,7 @@ struct DevBuf {
 struct Ctx {
     std::mutex mu;
     cudaStream_t stream = nullptr;
-    DevBuf in, out, ws;
+    DevBuf in, out, ws, fx, fx2;   // fx / fx2: fixed-rate search scratch and sample copies
     bool init() {
         if (stream) return true;
         return cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) == cudaSuccess;
@@ -197,7 +197,16 @@ static bool check_compress_args(int mode, int dtype, size_t n, int bs, int err_m
 // Host round trip: compress host values, stream back into a host buffer.
 // `out` == nullptr allocates with malloc.  Returns stream size, 0 on failure.
 static size_t host_compress(int mode, int dtype, const void* data, size_t n, int bs, int err_mode, float abs_eb,
-                            float rel, unsigned char** out, size_t out_cap) {
+                            float rel, unsigned char** out, size_t out_cap, float fxr_ratio = 0.f,
+                            float fxr_tolerance = 0.f) {
+    // fixed rate: the bound comes from the reference's search on the device,
+    // then the field is compressed into the fastMode-2 layout
+    // (szx/src/szx_float.cc:921-949, szx/src/szx.cc:240-243)
+    const bool fxr = err_mode == FXR;
+    if (fxr) {
+        mode = kBlocked;
+        err_mode = ABS;
+    }
     if (!data || !check_compress_args(mode, dtype, n, bs, err_mode)) { set_err(SZXG_ERR_ARG); return 0; }
     Ctx* c = ctx_for_device();
     if (!c) { set_err(SZXG_ERR_CUDA); return 0; }
@@ -225,6 +234,16 @@ static size_t host_compress(int mode, int dtype, const void* data, size_t n, int
     };
     cudaError_t e = cudaMemcpyAsync(c->in.p, data, n * es, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) { drop(); cuda_fail(e); return 0; }
+    if (fxr) {
+        const size_t fb = fxr_ws_bytes(dtype, n, bs, 10);
+        if (!c->fx.ensure(fb)) { drop(); set_err(SZXG_ERR_CUDA); return 0; }
+        if ((e = fxr_bound(dtype, c->in.p, n, bs, fxr_ratio, fxr_tolerance, c->fx.p, c->fx.cap, s, &abs_eb)) !=
+            cudaSuccess) {
+            drop();
+            cuda_fail(e);
+            return 0;
+        }
+    }
     if (enqueue_compress(mode, dtype, c->in.p, n, bs, err_mode, abs_eb, rel, (uint8_t*)c->out.p, c->out.cap, ws, s)) {
         drop();
         return 0;
@@ -409,13 +428,11 @@ int SZx_filterDimension(size_t r5, size_t r4, size_t r3, size_t r2, size_t r1, s
 unsigned char* SZx_fast_compress_args(int fastMode, int dataType, void* data, size_t* outSize, int errBoundMode,
                                       float absErrBound, float relBoundRatio, float compressionRatio, float tolerance,
                                       size_t r5, size_t r4, size_t r3, size_t r2, size_t r1) {
-    (void)compressionRatio;
-    (void)tolerance;
     if (outSize) *outSize = 0;
     const size_t n = SZx_computeDataLength(r5, r4, r3, r2, r1);
-    if (errBoundMode == FXR) { set_err(SZXG_ERR_UNSUPPORTED); return nullptr; }
     unsigned char* out = nullptr;
-    size_t sz = host_compress(fastMode, dataType, data, n, 128, errBoundMode, absErrBound, relBoundRatio, &out, 0);
+    size_t sz = host_compress(fastMode, dataType, data, n, 128, errBoundMode, absErrBound, relBoundRatio, &out, 0,
+                              compressionRatio, tolerance);
     if (!sz) return nullptr;
     if (outSize) *outSize = sz;
     return out;
@@ -496,29 +513,110 @@ void SZx_fast_decompress_args_unpredictable_blocked(void* newData, int dataType,
     set_err(SZXG_ERR_UNSUPPORTED);
 }
 
+// Stage n values of a host array on the device (Ctx input buffer).
+static bool stage_input(Ctx* c, const void* data, size_t bytes) {
+    if (!c->in.ensure(bytes)) return false;
+    return cudaMemcpyAsync(c->in.p, data, bytes, cudaMemcpyHostToDevice, c->stream) == cudaSuccess;
+}
+
+// szx/src/szx.cc:458-464.  The reference's model behind this entry point ends
+// the process (exit(0), szx/src/szx_float.cc:681, szx/src/szx_double.cc:678);
+// this one returns the bound its search settles on (0 on failure, with
+// SZxG_get_last_error() set).
 float SZx_estimateErrorBoundbasedonCR(int dataType, float targetCompressionRatio, float tolerance, void* data,
                                       float initErrorBound, int blockSize, size_t nbEle) {
-    (void)dataType; (void)targetCompressionRatio; (void)tolerance; (void)data; (void)initErrorBound;
-    (void)blockSize; (void)nbEle;
-    set_err(SZXG_ERR_UNSUPPORTED);
-    return 0.f;
+    if (!data || nbEle == 0 || blockSize < 1 || (dataType != 0 && dataType != 1)) { set_err(SZXG_ERR_ARG); return 0.f; }
+    Ctx* c = ctx_for_device();
+    if (!c) { set_err(SZXG_ERR_CUDA); return 0.f; }
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->init()) { set_err(SZXG_ERR_CUDA); return 0.f; }
+    const size_t es = dataType == 0 ? 4 : 8;
+    if (!stage_input(c, data, nbEle * es) || !c->fx.ensure(fxr_ws_bytes(dataType, nbEle, blockSize, 10))) {
+        set_err(SZXG_ERR_CUDA);
+        return 0.f;
+    }
+    float eb = 0.f;
+    cudaError_t e = fxr_bound_unbuffered(dataType, c->in.p, nbEle, blockSize, targetCompressionRatio, tolerance,
+                                         initErrorBound, c->fx.p, c->fx.cap, c->stream, &eb);
+    if (e != cudaSuccess) { cuda_fail(e); return 0.f; }
+    set_err(SZXG_OK);
+    return eb;
 }
 
+// szx/src/szx.cc:475-485: radius, median and a copy of every samplingRate-th
+// block (arrays malloc'd here, nbEle/(samplingRate*blockSize)+1 entries as
+// the reference allocates; the caller frees them).  `buffer` is a float** or
+// double** by data type.  Returns the sampled value range.
 float computeRadiusBuffer(void* oriData, int dataType, size_t nbEle, int samplingRate, int blockSize,
                           float** radiusArray, float** mediusArray, void* buffer) {
-    (void)oriData; (void)dataType; (void)nbEle; (void)samplingRate; (void)blockSize; (void)radiusArray;
-    (void)mediusArray; (void)buffer;
-    set_err(SZXG_ERR_UNSUPPORTED);
-    return 0.f;
+    if (!oriData || !radiusArray || !mediusArray || !buffer || nbEle == 0 || blockSize < 1 || samplingRate < 1 ||
+        (dataType != 0 && dataType != 1)) {
+        set_err(SZXG_ERR_ARG);
+        return 0.f;
+    }
+    Ctx* c = ctx_for_device();
+    if (!c) { set_err(SZXG_ERR_CUDA); return 0.f; }
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->init()) { set_err(SZXG_ERR_CUDA); return 0.f; }
+    const size_t es = dataType == 0 ? 4 : 8;
+    const size_t ns = nbEle / ((size_t)samplingRate * blockSize);
+    float* rads = (float*)malloc(sizeof(float) * (ns + 1));
+    float* meds = (float*)malloc(sizeof(float) * (ns + 1));
+    void* copy = malloc(es * (ns + 1) * blockSize);
+    if (!rads || !meds || !copy) {
+        free(rads); free(meds); free(copy);
+        set_err(SZXG_ERR_ARG);
+        return 0.f;
+    }
+    float range = 0.f;
+    cudaError_t e = cudaSuccess;
+    if (!stage_input(c, oriData, nbEle * es) || !c->fx.ensure(fxr_ws_bytes(dataType, nbEle, blockSize, samplingRate)) ||
+        !c->fx2.ensure(es * (ns + 1) * blockSize))
+        e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess)
+        e = fxr_radius_buffer(dataType, c->in.p, nbEle, samplingRate, blockSize, c->fx.p, c->fx.cap, c->fx2.p,
+                              c->stream, rads, meds, copy, &range);
+    if (e != cudaSuccess) {
+        free(rads); free(meds); free(copy);
+        cuda_fail(e);
+        return 0.f;
+    }
+    *radiusArray = rads;
+    *mediusArray = meds;
+    *(void**)buffer = copy;
+    set_err(SZXG_OK);
+    return range;
 }
 
+// szx/src/szx.cc:487-498: the ratio model at errorBound over the sampled
+// blocks computeRadiusBuffer returned.
 float estimateCRbasedonErrorBound_buffered(int dataType, float errorBound, void* buffer, float* medianArray,
                                           float* radiusArray, int samplingRate, int blockSize, size_t nbEle,
                                           size_t* sumReqNbBytes, size_t* sum_actual_leadNumbers) {
-    (void)dataType; (void)errorBound; (void)buffer; (void)medianArray; (void)radiusArray; (void)samplingRate;
-    (void)blockSize; (void)nbEle; (void)sumReqNbBytes; (void)sum_actual_leadNumbers;
-    set_err(SZXG_ERR_UNSUPPORTED);
-    return 0.f;
+    if (!buffer || !medianArray || !radiusArray || !sumReqNbBytes || !sum_actual_leadNumbers || nbEle == 0 ||
+        blockSize < 1 || samplingRate < 1 || (dataType != 0 && dataType != 1)) {
+        set_err(SZXG_ERR_ARG);
+        return 0.f;
+    }
+    Ctx* c = ctx_for_device();
+    if (!c) { set_err(SZXG_ERR_CUDA); return 0.f; }
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->init()) { set_err(SZXG_ERR_CUDA); return 0.f; }
+    const size_t es = dataType == 0 ? 4 : 8;
+    const size_t ns = nbEle / ((size_t)samplingRate * blockSize);
+    float cr = 0.f;
+    cudaError_t e = cudaSuccess;
+    if ((ns && !stage_input(c, buffer, es * ns * blockSize)) ||
+        !c->fx.ensure(fxr_ws_bytes(dataType, nbEle, blockSize, samplingRate)))
+        e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess && !c->in.p && !c->in.ensure(16)) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess)
+        e = fxr_estimate_buffered(dataType, c->in.p, nbEle, samplingRate, blockSize, radiusArray, medianArray,
+                                  errorBound, c->fx.p, c->fx.cap, c->stream, &cr, sumReqNbBytes,
+                                  sum_actual_leadNumbers);
+    if (e != cudaSuccess) { cuda_fail(e); return 0.f; }
+    set_err(SZXG_OK);
+    return cr;
 }
 
 // ------------------------------------------------------------------ SZxG device-pointer interface

@@ -100,6 +100,28 @@ constexpr size_t blocked_status_words(size_t nb) { return enc_status_words(nb) +
 void host_prefault_start(void* p, size_t n);
 void host_prefault_finish(size_t m);
 
+// ------------------------------------------------------------------ fixed-rate search (fxr.cu)
+
+// Device scratch of the searches below for n values, blocks of bs, every
+// rate-th block sampled.
+size_t fxr_ws_bytes(int dtype, size_t n, int bs, int rate);
+// Bound the reference's fixed-rate mode picks for the target ratio (buffered
+// model, started from 1% of the sampled range).  Synchronous on stream s.
+cudaError_t fxr_bound(int dtype, const void* d_x, size_t n, int bs, float ratio, float tolerance, void* d_ws,
+                      size_t wsb, cudaStream_t s, float* eb_out);
+// Search of SZx_estimateErrorBoundbasedonCR (unbuffered model) from initErrorBound.
+cudaError_t fxr_bound_unbuffered(int dtype, const void* d_x, size_t n, int bs, float ratio, float tolerance,
+                                 float initErrorBound, void* d_ws, size_t wsb, cudaStream_t s, float* eb_out);
+// computeRadiusBuffer: sampled radius / median / block copies into host arrays
+// (d_copy: device room for the copies); the sampled range in *range_out.
+cudaError_t fxr_radius_buffer(int dtype, const void* d_x, size_t n, int rate, int bs, void* d_ws, size_t wsb,
+                              void* d_copy, cudaStream_t s, float* h_rads, float* h_meds, void* h_copy,
+                              float* range_out);
+// estimateCRbasedonErrorBound_buffered over contiguous sampled blocks on the device.
+cudaError_t fxr_estimate_buffered(int dtype, const void* d_copy, size_t n, int rate, int bs, const float* h_rads,
+                                  const float* h_meds, float eb, void* d_ws, size_t wsb, cudaStream_t s, float* cr,
+                                  size_t* sumReq, size_t* sumLead);
+
 size_t ws_bytes(int layout, int dtype, size_t n, int bs);
 Workspace ws_carve(void* base, int layout, int dtype, size_t n, int bs);
 

@@ -90,9 +90,6 @@ def test_unsupported_paths_fail_cleanly_without_touching_the_gpu(L):
     import numpy as np
     x = np.zeros(16, np.float32)
     sz = C.c_size_t(123)
-    # FXR through the drop-in entry point is not available yet: NULL + code
-    p = L.SZx_fast_compress_args(3, 0, x.ctypes.data, C.byref(sz), 2, 0.0, 0.0, 4.0, 0.1, 0, 0, 0, 0, 16)
-    assert not p and sz.value == 0
     # bad arguments are rejected before any device work
     assert not L.SZx_fast_compress_args(7, 0, x.ctypes.data, C.byref(sz), 0, 1e-3, 0.0, 0.0, 0.0, 0, 0, 0, 0, 16)
     assert L.SZxG_get_last_error() == 4
