@@ -35,7 +35,7 @@ int sm_count() {
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct WsLayout {
-    size_t hdr, st32, st, st2, partials, o, m, s, p, rw, aux, total;
+    size_t hdr, st32, st, st2, partials, o, m, s, p, rw, aux, m2, m2_bytes, total;
     size_t status_tiles, status2_tiles, blocks, words, aux_tiles;
 };
 
@@ -62,6 +62,9 @@ static WsLayout ws_layout(int layout, int dtype, size_t n, int bs) {
     L.p = off; off += a256(8 * L.blocks);
     L.rw = off; off += a256(4 * L.words);
     L.aux = off; off += a256(3 * 8 * L.aux_tiles);
+    // fastMode 2 decode: boundary-search tables for the largest valid stream
+    L.m2_bytes = layout == kBlocked && bs > 0 ? m2_ws_bytes(dtype, n, bs, blocked_bound(kBlocked, dtype, n, bs)) : 0;
+    L.m2 = off; off += a256(L.m2_bytes);
     L.total = off;
     return L;
 }
@@ -94,6 +97,8 @@ Workspace ws_carve(void* base, int layout, int dtype, size_t n, int bs) {
     w.p_off = (unsigned long long*)(b + L.p);
     w.rank_w = (uint32_t*)(b + L.rw);
     w.tile_aux = (unsigned long long*)(b + L.aux);
+    w.m2 = b + L.m2;
+    w.m2_bytes = L.m2_bytes;
     w.status_tiles = L.status_tiles;
     w.status2_tiles = L.status2_tiles;
     w.blocks = L.blocks;
@@ -290,12 +295,16 @@ static uint64_t be64h(const unsigned char* p) {
 // Decode a host stream into host memory (`out` == nullptr: malloc).
 static void* host_decompress(int mode, int dtype, const unsigned char* bytes, size_t len, size_t n, void* out) {
     if (!bytes || n == 0 || (dtype != 0 && dtype != 1)) { set_err(SZXG_ERR_ARG); return nullptr; }
-    if (mode != kNonBlocked && mode != kRandomAccess && mode != kRandomAccessNative) {
+    if (!layout_ok(mode)) {
         set_err(SZXG_ERR_UNSUPPORTED);
         return nullptr;
     }
     int bs = 0;
-    if (mode != kNonBlocked) {
+    if (mode == kBlocked) {
+        if (len < 13) { set_err(SZXG_ERR_STREAM); return nullptr; }
+        bs = bytes[4];
+        if (bs < 1) { set_err(SZXG_ERR_STREAM); return nullptr; }
+    } else if (mode != kNonBlocked) {
         if (len < 20) { set_err(SZXG_ERR_STREAM); return nullptr; }
         uint64_t b = be64h(bytes + 4);
         if (b < 1 || b > 256) { set_err(b > 256 ? SZXG_ERR_UNSUPPORTED : SZXG_ERR_STREAM); return nullptr; }
@@ -504,13 +513,47 @@ size_t SZx_fast_compress_args_unpredictable_blocked_args(void* oriData, int data
                          blocked_bound(kBlocked, dataType, nbEle, blockSize));
 }
 
+// Length of a fastMode-2 stream of nbEle values, read from its block headers
+// (this entry point gets no length; the payload has no size index).  Only the
+// 1 + ceil(bs/4) header bytes of each non-constant block are read.  0 when
+// the bytes cannot be a stream.
+static size_t m2_stream_length(const unsigned char* b, size_t nbEle, int dataType) {
+    const size_t bs = b[4];
+    if (bs < 1 || b[3] != 0) return 0;
+    const size_t nb = (nbEle + bs - 1) / bs, sb = (nb + 7) / 8;
+    const size_t nc = (size_t)be64h(b + 5);
+    if (nc > nb) return 0;
+    size_t nnc = 0;
+    for (size_t i = 0; i < sb; i++) nnc += (size_t)__builtin_popcount(b[13 + i]);
+    if (nnc + nc != nb) return 0;   // also rejects set padding bits
+    const int lo = dataType == 0 ? 9 : 12, hi = dataType == 0 ? 32 : 64;
+    size_t p = 13 + sb + 4 * nc;
+    const bool last_coded = (b[13 + (nb - 1) / 8] >> (7 - (nb - 1) % 8)) & 1;
+    for (size_t r = 0; r < nnc; r++) {
+        const size_t blen = (r + 1 == nnc && last_coded) ? nbEle - (nb - 1) * bs : bs;
+        const int rl = b[p];
+        if (rl < lo || rl > hi) return 0;
+        const int R = (rl >> 3) + ((rl & 7) != 0);
+        const size_t Lb = (blen + 3) / 4;
+        size_t mid = 0;
+        for (size_t v = 0; v < blen; v++) {
+            const int ld = (b[p + 5 + v / 4] >> (6 - 2 * (v % 4))) & 3;
+            mid += R > ld ? (size_t)(R - ld) : 0;
+        }
+        p += 5 + Lb + mid;
+    }
+    return p;
+}
+
+// szx/src/szx.cc:513-520: fastMode-2 stream -> *newData (a float** or
+// double** by type, malloc'd here as the reference does).
 void SZx_fast_decompress_args_unpredictable_blocked(void* newData, int dataType, size_t nbEle,
                                                    unsigned char* cmpBytes) {
-    (void)newData;
-    (void)dataType;
-    (void)nbEle;
-    (void)cmpBytes;
-    set_err(SZXG_ERR_UNSUPPORTED);
+    if (!newData || !cmpBytes || nbEle == 0 || (dataType != 0 && dataType != 1)) { set_err(SZXG_ERR_ARG); return; }
+    const size_t len = m2_stream_length(cmpBytes, nbEle, dataType);
+    if (!len) { set_err(SZXG_ERR_STREAM); return; }
+    void* out = host_decompress(kBlocked, dataType, cmpBytes, len, nbEle, nullptr);
+    if (out) *(void**)newData = out;
 }
 
 // Stage n values of a host array on the device (Ctx input buffer).
@@ -660,12 +703,20 @@ int SZxG_decompress(int fastMode, int dataType, const void* d_stream, size_t str
         set_err(SZXG_ERR_ARG);
         return SZXG_ERR_ARG;
     }
-    if (fastMode != kNonBlocked && fastMode != kRandomAccess && fastMode != kRandomAccessNative) {
+    if (!layout_ok(fastMode)) {
         set_err(SZXG_ERR_UNSUPPORTED);
         return SZXG_ERR_UNSUPPORTED;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    if (fastMode != kNonBlocked && blockSize == 0) {
+    if (fastMode == kBlocked && blockSize == 0) {
+        unsigned char h[5];
+        if (streamBytes < 13 || cudaMemcpyAsync(h, d_stream, 5, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess || h[4] < 1) {
+            set_err(SZXG_ERR_STREAM);
+            return SZXG_ERR_STREAM;
+        }
+        blockSize = h[4];
+    } else if (fastMode != kNonBlocked && blockSize == 0) {
         unsigned char h[12];
         if (streamBytes < 20 || cudaMemcpyAsync(h, d_stream, 12, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess) {

@@ -735,7 +735,7 @@ __global__ void __launch_bounds__(kIdxThreads) k_blocked_index(const uint8_t* s,
                                                                unsigned long long* P, uint32_t* RW,
                                                                TileStatus stA, TileStatus stB,
                                                                unsigned long long* ctr, int* err,
-                                                               unsigned long long len) {
+                                                               unsigned long long len, int famA) {
     __shared__ unsigned long long sm[8];
     __shared__ long long s_tile;
     __shared__ unsigned long long s_base;
@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(kIdxThreads) k_blocked_index(const uint8_t* s,
     if (!h.ok) return;
     constexpr unsigned long long per = (unsigned long long)kIdxThreads * kIdxItems;
     const unsigned long long nw = (h.nb + 31) / 32;
-    const long long TA = (long long)((h.nnc + per - 1) / per);
+    const long long TA = famA ? (long long)((h.nnc + per - 1) / per) : 0;   // no size index in fastMode 2
     const long long TBt = (long long)((nw + per - 1) / per);
     for (;;) {
         if (threadIdx.x == 0) s_tile = (long long)atomicAdd(ctr, 1ull);
@@ -1201,15 +1201,17 @@ static cudaError_t run_decode(const uint8_t* s, size_t len, size_t nb, const Wor
 
 cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream, size_t len, size_t n, int bs,
                                   void* d_out, const Workspace& ws, cudaStream_t s) {
-    if (layout != kRandomAccess && layout != kRandomAccessNative) return cudaErrorInvalidValue;
+    if (layout != kBlocked && layout != kRandomAccess && layout != kRandomAccessNative) return cudaErrorInvalidValue;
     if (bs < 1 || bs > 256 || n == 0) return cudaErrorInvalidValue;
+    const bool m2 = layout == kBlocked;
     cudaError_t e;
     if ((e = cudaMemsetAsync(ws.counters, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ws.st_word, 0, sizeof(unsigned long long) * ws.status_tiles, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ws.st2_word, 0, sizeof(unsigned long long) * ws.status2_tiles, s)) != cudaSuccess) return e;
     {
         TraceScope tr("blocked_parse", s);
-        k_blocked_parse<<<1, 1, 0, s>>>(d_stream, len, n, (unsigned long long)bs, ws.bhdr, ws.err);
+        if (m2) k_m2_parse<<<1, 1, 0, s>>>(d_stream, len, n, (unsigned long long)bs, ws.bhdr, ws.err);
+        else k_blocked_parse<<<1, 1, 0, s>>>(d_stream, len, n, (unsigned long long)bs, ws.bhdr, ws.err);
     }
     {
         int ig = sm_count() * 4;
@@ -1217,8 +1219,10 @@ cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream
         k_blocked_index<<<ig, kIdxThreads, 0, s>>>(d_stream, ws.bhdr, ws.p_off, ws.rank_w,
                                                     TileStatus{ws.st_word, ws.st_agg2, ws.st_inc2},
                                                     TileStatus{ws.st2_word, ws.st2_agg2, ws.st2_inc2},
-                                                    &ws.counters[0], ws.err, len);
+                                                    &ws.counters[0], ws.err, len, m2 ? 0 : 1);
     }
+    if (m2 && (e = launch_m2_offsets(dtype, d_stream, len, n, bs, ws.m2, ws.m2_bytes, ws, s)) != cudaSuccess)
+        return e;
     // bs comes from the stream header (read by the caller); the device header
     // is validated again by every kernel and a mismatch is reported, not used.
     const int native = layout == kRandomAccessNative;

@@ -79,6 +79,8 @@ struct Workspace {
     unsigned long long* p_off;      // decode: payload offsets by non-constant rank
     uint32_t* rank_w;               // decode: non-constant rank at each 32-block word
     unsigned long long* tile_aux;   // non-blocked decode: per-tile summaries
+    void* m2;                       // fastMode-2 decode: block-boundary search tables
+    size_t m2_bytes;
     size_t status_tiles, status2_tiles, blocks, words, aux_tiles;
 };
 
@@ -121,6 +123,15 @@ cudaError_t fxr_radius_buffer(int dtype, const void* d_x, size_t n, int rate, in
 cudaError_t fxr_estimate_buffered(int dtype, const void* d_copy, size_t n, int rate, int bs, const float* h_rads,
                                   const float* h_meds, float eb, void* d_ws, size_t wsb, cudaStream_t s, float* cr,
                                   size_t* sumReq, size_t* sumLead);
+
+// Scratch of the fastMode-2 boundary search for a stream of len bytes (mode2.cu).
+size_t m2_ws_bytes(int dtype, size_t n, int bs, size_t len);
+// Payload offsets of a fastMode-2 stream by non-constant rank into ws.p_off
+// (header already parsed into ws.bhdr).
+cudaError_t launch_m2_offsets(int dtype, const uint8_t* d_stream, size_t len, size_t n, int bs, void* m2ws,
+                              size_t m2wsb, const Workspace& ws, cudaStream_t s);
+__global__ void k_m2_parse(const uint8_t* s, unsigned long long len, unsigned long long n,
+                           unsigned long long bs_expect, BlockedHdr* h, int* err);
 
 size_t ws_bytes(int layout, int dtype, size_t n, int bs);
 Workspace ws_carve(void* base, int layout, int dtype, size_t n, int bs);

@@ -94,5 +94,6 @@ def test_unsupported_paths_fail_cleanly_without_touching_the_gpu(L):
     assert not L.SZx_fast_compress_args(7, 0, x.ctypes.data, C.byref(sz), 0, 1e-3, 0.0, 0.0, 0.0, 0, 0, 0, 0, 16)
     assert L.SZxG_get_last_error() == 4
     assert not L.SZx_fast_compress_args(3, 5, x.ctypes.data, C.byref(sz), 0, 1e-3, 0.0, 0.0, 0.0, 0, 0, 0, 0, 16)
+    # a fastMode-2 stream whose block size byte is 0 is malformed
     assert not L.SZx_fast_decompress(2, 0, x.ctypes.data, 64, 0, 0, 0, 0, 16)
-    assert L.SZxG_get_last_error() == 6
+    assert L.SZxG_get_last_error() == 3

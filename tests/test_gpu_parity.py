@@ -50,8 +50,6 @@ def test_golden_streams_bit_exact(szx, golden):
 
 def test_golden_decode_bit_exact(szx, golden):
     for c in golden:
-        if c["mode"] == 2:
-            continue
         y = szx.decompress_host(c["mode"], c["x"].dtype, c["stream"], c["n"])
         z = O.decompress(c["mode"], c["x"].dtype, c["stream"], c["n"])
         assert same_bits(y, z), c["name"]
@@ -95,8 +93,6 @@ def test_seeded_fields_match_oracle(szx, dt, kind):
             want = O.fast_compress_args(mode, x, err_mode, eb, rel, bs)
             got = szx.compress_host(mode, x, bs, err_mode, eb, rel)
             assert got == want, (kind, mode, bs, err_mode, rel)
-            if mode == 2:
-                continue
             y = szx.decompress_host(mode, dt, got, n)
             z = O.decompress(mode, dt, want, n)
             assert same_bits(y, z), (kind, mode, bs, err_mode, rel)
@@ -108,10 +104,11 @@ def test_every_block_size_and_ragged_length(szx, dt):
     for bs in (1, 2, 3, 5, 8, 31, 32, 33, 63, 64, 65, 100, 127, 128, 129, 200, 255, 256):
         for n in (1, 2, bs, bs + 1, 3 * bs - 1, 4097):
             x = (np.sin(np.arange(n) / 17.0) + rng.normal(0, 1e-2, n)).astype(dt)
-            want = O.compress(3, x, 1e-3, bs)
-            got = szx.compress_host(3, x, bs, 0, 1e-3, 0.0)
-            assert got == want, (bs, n)
-            assert same_bits(szx.decompress_host(3, dt, got, n), O.decompress(3, dt, want, n)), (bs, n)
+            for mode in ((3, 2) if bs <= 255 else (3,)):
+                want = O.compress(mode, x, 1e-3, bs)
+                got = szx.compress_host(mode, x, bs, 0, 1e-3, 0.0)
+                assert got == want, (mode, bs, n)
+                assert same_bits(szx.decompress_host(mode, dt, got, n), O.decompress(mode, dt, want, n)), (mode, bs, n)
 
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
@@ -119,7 +116,7 @@ def test_tiny_arrays_all_modes(szx, dt):
     rng = np.random.default_rng(23)
     for n in (1, 2, 3, 4, 5, 15, 16, 17, 127, 128, 129, 4095, 4096, 4097, 8193):
         x = rng.normal(size=n).astype(dt)
-        for mode in (1, 3, 4):
+        for mode in (1, 2, 3, 4):
             want = O.compress(mode, x, 1e-2, 128)
             got = szx.compress_host(mode, x, 128, 0, 1e-2, 0.0)
             assert got == want, (n, mode)
@@ -205,3 +202,51 @@ def test_corrupt_and_truncated_streams_fail_cleanly(szx):
         szx.fast_decompress(1, np.float32, s1[: len(s1) - 1000], x.size)
     # the library still works afterwards
     assert szx.fast_compress_args(3, x, 0, 1e-3) == s
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_mode2_decode_large_and_periodic(szx, dt):
+    """fastMode 2 has no size index: block boundaries come from a parallel
+    speculative search.  A large field exercises many segments; a periodic
+    field (identical blocks) makes false walks survive in step with the true
+    one, which the search must detect and repair."""
+    rng = np.random.default_rng(31)
+    n = 3_000_017
+    x = (np.cumsum(rng.normal(size=n)) * 1e-2).astype(dt)
+    for eb in (1e-4, 1e-2):
+        s = szx.compress_host(2, x, 128, 0, eb, 0.0)
+        assert s == O.compress(2, x, eb, 128)
+        assert same_bits(szx.decompress_host(2, dt, s, n), O.decompress(2, dt, s, n)), eb
+    tile = rng.normal(size=128 * 7).astype(dt)
+    xp = np.tile(tile, 4000)
+    s = szx.compress_host(2, xp, 128, 0, 1e-3, 0.0)
+    assert s == O.compress(2, xp, 1e-3, 128)
+    assert same_bits(szx.decompress_host(2, dt, s, xp.size), O.decompress(2, dt, s, xp.size))
+
+
+def test_mode2_entry_point_without_length(szx):
+    """SZx_fast_decompress_args_unpredictable_blocked takes no stream length."""
+    import ctypes as C
+    from szx_gb300._lib import lib, libc
+    rng = np.random.default_rng(37)
+    for dt, code in ((np.float32, 0), (np.float64, 1)):
+        x = rng.normal(size=100_003).astype(dt)
+        s = np.frombuffer(O.compress(2, x, 1e-2, 128), np.uint8).copy()
+        out = C.c_void_p()
+        lib().SZx_fast_decompress_args_unpredictable_blocked(C.byref(out), code, x.size, s.ctypes.data)
+        assert out.value
+        y = np.frombuffer(C.string_at(out.value, x.nbytes), dt).copy()
+        libc().free(out)
+        assert same_bits(y, O.decompress(2, dt, s.tobytes(), x.size))
+
+
+def test_fixed_rate_round_trip_within_the_bound(szx):
+    """A fixed-rate stream (fastMode-2 layout) decodes through the drop-in
+    entry point within the bound the search chose."""
+    rng = np.random.default_rng(41)
+    x = (np.cumsum(rng.normal(size=1 << 20)) * 1e-2).astype(np.float32)
+    for ratio in (4.0, 8.0, 16.0):
+        s = szx.fast_compress_args(3, x, 2, compressionRatio=ratio, tolerance=0.1)
+        eb = O.fxr_bound(x, ratio, 0.1)
+        y = szx.fast_decompress(2, np.float32, s, x.size)
+        assert np.max(np.abs(y.astype(np.float64) - x)) <= eb * (1 + 1e-6), ratio
