@@ -174,6 +174,42 @@ size_t SZxG_compress_host_into(int fastMode, int dataType, const void* data, siz
 int SZxG_decompress_host_into(int fastMode, int dataType, const unsigned char* bytes, size_t byteLength, size_t nbEle,
                               void* out);
 
+/* ---------------------------------------------------------------- batches
+ * Many fields of one type and block size coded by ONE persistent launch per
+ * kernel over a device work queue of (field, block-range) tiles, instead of
+ * a launch sequence per field (no counterpart in the reference, which codes
+ * one array per call; each field's stream is exactly what
+ * SZx_fast_compress_args / SZxG_compress would produce for it).
+ *
+ * SZxG_batch_create plans the batch once: it checks the fields, lays out
+ * every field's scratch, allocates it (one cudaMalloc) and uploads the field
+ * table.  SZxG_batch_run then only enqueues memsets, kernels and (optionally)
+ * a device-to-device copy of the per-field results on `stream`, so it can be
+ * captured into a CUDA graph and replayed; the fields' buffers must stay
+ * valid while the plan is used.  Runs of one plan must not overlap. */
+typedef struct {
+    const void* in;          /* compress: nbEle values (device); decompress: the stream (device) */
+    size_t nbEle;            /* values */
+    size_t inBytes;          /* decompress: stream bytes; compress: ignored */
+    float absErrBound;       /* compress: absolute bound */
+    int reserved;
+    void* out;               /* compress: stream buffer, >= SZxG_compress_bound bytes; decompress: nbEle values */
+    size_t outCapacity;      /* bytes at out */
+} SZxG_Field;
+
+typedef struct SZxG_Batch SZxG_Batch;
+
+/* direction 0: compress (fastMode 2, 3, 4); 1: decompress (fastMode 3, 4).
+ * Returns NULL on failure (SZxG_get_last_error). */
+SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blockSize, int nFields,
+                              const SZxG_Field* fields);
+/* Enqueue the batch; compress results (stream at out + offset) go to
+ * d_info[nFields] when d_info is not NULL. */
+int SZxG_batch_run(SZxG_Batch* batch, SZxG_StreamInfo* d_info, void* stream);
+/* Wait for `stream` and report the batch's error word (0: all fields fine). */
+int SZxG_batch_status(SZxG_Batch* batch, void* stream);
+void SZxG_batch_destroy(SZxG_Batch* batch);
+
 /* Launch tracing: CUDA events around every kernel this library enqueues.
  * enable(1) starts (and clears) a trace, enable(0) stops and clears it.
  * collect() waits for the recorded events and writes, per kernel name, the

@@ -114,6 +114,7 @@ static const size_t kWsErrOff = 448, kWsResultOff = 128;
 
 static thread_local int g_last_error = SZXG_OK;
 static void set_err(int e) { g_last_error = e; }
+void set_last_error(int e) { g_last_error = e; }
 
 // ------------------------------------------------------------------ per-device context
 

@@ -1,0 +1,170 @@
+// Batches: many fields of one type and block size coded by one persistent
+// launch per kernel over a device work queue of (field, block-range) tiles.
+//
+// The blocked kernels take a table of fields (a single-field call is a table
+// of one): a launch-wide tile index maps to (field, local tile) by a binary
+// search over the fields' first tiles, and every field keeps its own
+// look-back status words, totals, scratch and stream.  Tiles are handed out
+// in field order from one atomic counter, so a field's tiles are always
+// acquired before any later field's, which is all the per-field look-back
+// needs to make progress.  This file plans a batch (layout of the per-field
+// scratch in one allocation, the field table on the device) and runs it as a
+// handful of memsets and launches that a CUDA graph can capture.
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/szx_gb300.h"
+#include "kernels.h"
+
+using namespace szxg;
+
+struct SZxG_Batch {
+    int direction, mode, dtype, bs, nf;
+    void* dev = nullptr;
+    BlkField* d_fields = nullptr;     // device table (nf > 1)
+    BlkField one;                     // the field when nf == 1
+    StreamResult* results = nullptr;
+    unsigned long long* counters = nullptr;   // [0..3] tile counters, then the error word
+    int* err = nullptr;
+    uint8_t* zero = nullptr;          // status words and totals of every field
+    size_t zero_bytes = 0;
+    unsigned long long enc_total = 0, asm_total = 0;
+};
+
+namespace {
+
+size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+SZxG_Batch* fail(int code) {
+    set_last_error(code);
+    return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blockSize, int nFields,
+                              const SZxG_Field* fields) {
+    if (direction == 1) return fail(SZXG_ERR_UNSUPPORTED);
+    if (direction != 0 || nFields < 1 || !fields || (dataType != 0 && dataType != 1)) return fail(SZXG_ERR_ARG);
+    if (fastMode != kBlocked && fastMode != kRandomAccess && fastMode != kRandomAccessNative)
+        return fail(SZXG_ERR_UNSUPPORTED);
+    if (blockSize < 1 || blockSize > 256 || (fastMode == kBlocked && blockSize > 255)) return fail(SZXG_ERR_ARG);
+    const size_t nf = (size_t)nFields;
+    const size_t tb = (size_t)blocked_tile_blocks(dataType, blockSize);
+    const size_t hdr = fastMode == kBlocked ? 13 : 20;
+    // layout: table | results | counters+err | zeroed status words and totals | scratch
+    size_t off = 0;
+    const size_t o_tab = off; off += a256(sizeof(BlkField) * nf);
+    const size_t o_res = off; off += a256(sizeof(StreamResult) * nf);
+    const size_t o_ctr = off; off += 256;
+    const size_t o_zero = off;
+    std::vector<size_t> o_st(nf), o_tot(nf), o_sz(nf), o_md(nf), o_ss(nf);
+    for (size_t f = 0; f < nf; f++) {
+        const SZxG_Field& F = fields[f];
+        if (!F.in || !F.out || F.nbEle == 0) return fail(SZXG_ERR_ARG);
+        const size_t nb = (F.nbEle + blockSize - 1) / blockSize;
+        if (F.outCapacity < blocked_bound(fastMode, dataType, F.nbEle, blockSize)) return fail(SZXG_ERR_CAPACITY);
+        o_st[f] = off; off += a256(8 * blocked_status_words(nb));
+    }
+    for (size_t f = 0; f < nf; f++) { o_tot[f] = off; off += 64; }
+    off = a256(off);
+    const size_t zero_bytes = off - o_zero;
+    for (size_t f = 0; f < nf; f++) {
+        const size_t nb = (fields[f].nbEle + blockSize - 1) / blockSize;
+        o_sz[f] = off; off += a256(2 * nb);
+        o_md[f] = off; off += a256(4 * nb);
+        o_ss[f] = off; off += a256(nb / 8 + 64);
+    }
+    SZxG_Batch* b = new SZxG_Batch();
+    b->direction = direction; b->mode = fastMode; b->dtype = dataType; b->bs = blockSize; b->nf = nFields;
+    if (cudaMalloc(&b->dev, off) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return fail(SZXG_ERR_CUDA);
+    }
+    uint8_t* base = (uint8_t*)b->dev;
+    b->results = (StreamResult*)(base + o_res);
+    b->counters = (unsigned long long*)(base + o_ctr);
+    b->err = (int*)(base + o_ctr + 64);
+    b->zero = base + o_zero;
+    b->zero_bytes = zero_bytes;
+    std::vector<BlkField> tab(nf);
+    unsigned long long et = 0, at = 0;
+    for (size_t f = 0; f < nf; f++) {
+        const SZxG_Field& S = fields[f];
+        const size_t nb = (S.nbEle + blockSize - 1) / blockSize, sb = (nb + 7) / 8;
+        const size_t qfix = hdr + sb + 4 * nb;
+        BlkField& F = tab[f];
+        memset(&F, 0, sizeof F);
+        F.x = S.in; F.n = S.nbEle; F.nb = nb;
+        F.enc_tiles = (nb + tb - 1) / tb; F.enc_tile0 = et; et += F.enc_tiles;
+        F.asm_tiles = (nb + kAsmBlocksPerTile - 1) / kAsmBlocksPerTile; F.asm_tile0 = at; at += F.asm_tiles;
+        F.eb = S.absErrBound;
+        F.params = nullptr;
+        F.out = (uint8_t*)S.out;
+        F.payload = F.out + qfix;
+        F.payload_cap = S.outCapacity - qfix;
+        F.st_enc = (unsigned long long*)(base + o_st[f]);
+        F.st_asm = F.st_enc + enc_status_words(nb);
+        F.size_blk = (uint16_t*)(base + o_sz[f]);
+        F.med_blk = (uint32_t*)(base + o_md[f]);
+        F.s_scr = base + o_ss[f];
+        F.tot = (Totals*)(base + o_tot[f]);
+        F.res = b->results + f;
+    }
+    b->enc_total = et;
+    b->asm_total = at;
+    b->one = tab[0];
+    b->d_fields = (BlkField*)(base + o_tab);
+    if (cudaMemcpy(b->d_fields, tab.data(), sizeof(BlkField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(b->dev);
+        delete b;
+        return fail(SZXG_ERR_CUDA);
+    }
+    set_last_error(SZXG_OK);
+    return b;
+}
+
+int SZxG_batch_run(SZxG_Batch* b, SZxG_StreamInfo* d_info, void* stream) {
+    if (!b) { set_last_error(SZXG_ERR_ARG); return SZXG_ERR_ARG; }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(b->zero, 0, b->zero_bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->counters, 0, 128, s);
+    if (e == cudaSuccess)
+        e = launch_blocked_encode_fields(b->mode, b->dtype, b->bs, b->nf, b->one, b->nf > 1 ? b->d_fields : nullptr,
+                                         b->enc_total, b->asm_total, b->counters, b->err, s);
+    if (e == cudaSuccess && d_info)
+        e = cudaMemcpyAsync(d_info, b->results, sizeof(StreamResult) * b->nf, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error(SZXG_ERR_CUDA);
+        return SZXG_ERR_CUDA;
+    }
+    set_last_error(SZXG_OK);
+    return SZXG_OK;
+}
+
+int SZxG_batch_status(SZxG_Batch* b, void* stream) {
+    if (!b) return SZXG_ERR_ARG;
+    int h = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(&h, b->err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        return SZXG_ERR_CUDA;
+    }
+    return h;
+}
+
+void SZxG_batch_destroy(SZxG_Batch* b) {
+    if (!b) return;
+    if (b->dev) cudaFree(b->dev);
+    delete b;
+}
+
+}  // extern "C"

@@ -60,21 +60,14 @@ struct BlockEnc {
 };
 
 struct EncArgs {
-    unsigned long long* st64;    // tile status, [ntiles + 4]
-    const void* x;
-    unsigned long long n, nb, ntiles;
+    BlkField one;                // the field when nf == 1
+    const BlkField* fields;      // nf > 1: device table in ascending enc_tile0
+    int nf;
     int bs;
     int omp_stats;               // mode-4 double statistics
-    float eb;
-    const CodecParams* params;   // when set, params->eb overrides eb
-    uint8_t* payload;            // fixed position of the payload region
-    unsigned long long payload_cap;
-    uint16_t* size_blk;          // [nb] payload bytes by block (0: constant)
-    uint32_t* med_blk;           // [nb] stored median by block
-    uint8_t* s_scr;              // state bits
+    unsigned long long total_tiles;
     unsigned long long* tile_ctr;
     int* err;
-    Totals* tot;
 };
 
 // Statistics pass of one block by a G-lane segment: state, reqLength and
@@ -274,7 +267,7 @@ struct EncTile {
 // A segment of G lanes owns one block from its statistics to its emission;
 // the look-back of a tile runs one tile later than its publication, so
 // predecessors have normally published by then.
-template <typename T, int G>
+template <typename T, int G, bool MULTI>
 __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     using TL = EncTile<T, G>;
     constexpr int TB = TL::kBlocks;
@@ -287,34 +280,51 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     __shared__ uint32_t s_size[2][TB], s_med[2][TB], s_loc[2][TB];
     __shared__ uint8_t s_state[2][TB];
     __shared__ uint32_t s_agg[2];
-    __shared__ long long s_tile[2];
+    __shared__ long long s_tile[2];     // launch-wide tile index held by each input buffer
+    __shared__ int s_fld[2];            // its field
     __shared__ unsigned long long s_base;
     __shared__ int s_skip;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int seg = lane / G, sl = lane & (G - 1);
-    const T* x = (const T*)a.x;
-    const float eb = a.params ? a.params->eb : a.eb;
-    const long long nt = (long long)a.ntiles;
+    const long long nt = (long long)a.total_tiles;
     const unsigned long long tile_elems = (unsigned long long)TB * a.bs;
-    const bool tma_ok = ((uintptr_t)x & 15) == 0;
     const bool vec = ((a.bs * (int)sizeof(T)) & 15) == 0;   // every block starts 16-byte aligned
+    // field of a launch-wide tile (fields in ascending enc_tile0)
+    auto field_of = [&](long long g) {
+        int lo = 0, hi = a.nf - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((long long)a.fields[mid].enc_tile0 <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    };
     if (threadIdx.x == 0) {
         for (int i = 0; i < 2; i++) mbar_init(&bar[i], 1);
         mbar_fence_init();
-        s_tile[0] = (long long)atomicAdd(a.tile_ctr, 1ull);
-        s_tile[1] = (long long)atomicAdd(a.tile_ctr, 1ull);
+        for (int i = 0; i < 2; i++) {
+            s_tile[i] = (long long)atomicAdd(a.tile_ctr, 1ull);
+            s_fld[i] = (MULTI && s_tile[i] < nt) ? field_of(s_tile[i]) : 0;
+        }
     }
     __syncthreads();
+    // a field's members: from the kernel parameters for one field, from the table for a batch
+    auto fld = [&](int f) -> const BlkField* { return MULTI ? a.fields + f : nullptr; };
+#define FV(F_, m) (MULTI ? (F_)->m : a.one.m)
     uint32_t phase = 0;   // bit i: parity to wait for on input buffer i
 
-    auto tile_count = [&](long long t) {
+    auto tile_count = [&](const BlkField* F, long long t) {
         const unsigned long long start = (unsigned long long)t * tile_elems;
-        const unsigned long long rem = a.n - start;
+        const unsigned long long rem = FV(F, n) - start;
         return rem < tile_elems ? rem : tile_elems;
     };
-    auto issue = [&](long long t, int which) {
-        const unsigned long long cnt = tile_count(t);
+    auto issue = [&](long long g, int f, int which) {
+        const BlkField* F = fld(f);
+        const long long t = g - (long long)FV(F, enc_tile0);
+        const T* x = (const T*)FV(F, x);
+        const bool tma_ok = ((uintptr_t)x & 15) == 0;
+        const unsigned long long cnt = tile_count(F, t);
         const uint32_t bytes = (uint32_t)(cnt * sizeof(T));
         const uint32_t tbytes = tma_ok ? (bytes & ~15u) : 0u;
         T* dst = (T*)(inb + which * TL::kIn);
@@ -326,25 +336,25 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         }
         for (unsigned long long i = tbytes / sizeof(T) + threadIdx.x; i < cnt; i += kEncThreads) dst[i] = src[i];
     };
-    auto wait_buf = [&](long long t, int which) {
-        if (tma_ok && ((tile_count(t) * sizeof(T)) & ~15ull)) {
+    auto wait_buf = [&](const BlkField* F, long long t, int which) {
+        if (((uintptr_t)FV(F, x) & 15) == 0 && ((tile_count(F, t) * sizeof(T)) & ~15ull)) {
             if (!mbar_wait(&bar[which], (phase >> which) & 1u) && threadIdx.x == 0) atomicExch(a.err, kErrLookback);
             phase ^= 1u << which;
         }
     };
-    auto block_len = [&](long long t, int lb) {
+    auto block_len = [&](const BlkField* F, long long t, int lb) {
         const unsigned long long b = (unsigned long long)t * TB + lb;
-        if (b >= a.nb) return 0;
-        const unsigned long long rem = a.n - b * (unsigned long long)a.bs;
+        if (b >= FV(F, nb)) return 0;
+        const unsigned long long rem = FV(F, n) - b * (unsigned long long)a.bs;
         return rem < (unsigned long long)a.bs ? (int)rem : a.bs;
     };
 
-    unsigned long long nnc_cta = 0;   // warp 0 lane 0: non-constant blocks of this CTA's tiles
-    // warp 0: offset of tile t (slot), its sizes / medians / state bits by block
-    auto resolve = [&](long long t, int slot) {
+    unsigned long long nnc_cta = 0;   // warp 0 lane 0, single field: non-constant blocks of this CTA's tiles
+    // warp 0: offset of tile t of field F (slot), its sizes / medians / state bits by block
+    auto resolve = [&](const BlkField* F, long long t, int slot) {
         const uint32_t agg = s_agg[slot];
-        const unsigned long long base = prefix_resolve(a.st64, t, agg, a.err);
-        const bool cap_ok = base + agg <= a.payload_cap;
+        const unsigned long long base = prefix_resolve(FV(F, st_enc), t, agg, a.err);
+        const bool cap_ok = base + agg <= FV(F, payload_cap);
         const unsigned long long tb0 = (unsigned long long)t * TB;
         uint32_t m01[2];
 #pragma unroll
@@ -353,45 +363,52 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
             const bool in = lb < TB;
             const int st = in ? s_state[slot][lb] : 2;
             if (in && st != 2) {
-                a.size_blk[tb0 + lb] = (uint16_t)s_size[slot][lb];
-                a.med_blk[tb0 + lb] = s_med[slot][lb];
+                FV(F, size_blk)[tb0 + lb] = (uint16_t)s_size[slot][lb];
+                FV(F, med_blk)[tb0 + lb] = s_med[slot][lb];
             }
             m01[h] = __ballot_sync(0xffffffffu, in && st == 1);
         }
         if (lane == 0) {
             // state bits, MSB first (szx/src/szx_TypeManager.cc:16-40)
-            uint8_t* sbp = a.s_scr + (unsigned long long)t * (TB / 8);
+            uint8_t* sbp = FV(F, s_scr) + (unsigned long long)t * (TB / 8);
             const uint32_t r0 = __brev(m01[0]), r1 = __brev(m01[1]);
 #pragma unroll
             for (int k = 0; k < TB / 8; k++) sbp[k] = (uint8_t)((k < 4 ? r0 : r1) >> (24 - 8 * (k & 3)));
             if (!cap_ok) atomicExch(a.err, kErrCapacity);
-            nnc_cta += (unsigned long long)(__popc(m01[0]) + __popc(m01[1]));
-            if (t == nt - 1) a.tot->payload_bytes = base + agg;
+            const unsigned long long k = (unsigned long long)(__popc(m01[0]) + __popc(m01[1]));
+            if (!MULTI) nnc_cta += k;
+            else if (k) atomicAdd(&FV(F, tot)->nnc, k);
+            if (t == (long long)FV(F, enc_tiles) - 1) FV(F, tot)->payload_bytes = base + agg;
             s_base = base;
             s_skip = !cap_ok;
         }
     };
 
     {
-        const long long t0 = s_tile[0], t1 = s_tile[1];
-        if (t0 < nt) issue(t0, 0);
-        if (t1 < nt) issue(t1, 1);
+        const long long g0 = s_tile[0], g1 = s_tile[1];
+        if (g0 < nt) issue(g0, s_fld[0], 0);
+        if (g1 < nt) issue(g1, s_fld[1], 1);
     }
     long long t_prev = -1;
+    int f_prev = 0;
     int i = 0;
     for (;; i++) {
         const int slot = i & 1;
         __syncthreads();   // s_tile of this slot, previous copy-out done
-        const long long t = s_tile[slot];
-        if (t >= nt) break;
-        wait_buf(t, slot);
+        const long long g = s_tile[slot];
+        if (g >= nt) break;
+        const int f = s_fld[slot];
+        const BlkField* F = fld(f);
+        const long long t = g - (long long)FV(F, enc_tile0);
+        wait_buf(F, t, slot);
         // ---- statistics of the tile's blocks, one block per segment
         const int lb = warp * BPW + seg;
         const bool mine = warp < NGRP;
-        const int len = mine ? block_len(t, lb) : 0;
+        const int len = mine ? block_len(F, t, lb) : 0;
         const bool full = __all_sync(0xffffffffu, len == TL::kBsMax);
         BlockEnc<T> b;
         if (mine) {
+            const float eb = FV(F, params) ? FV(F, params)->eb : FV(F, eb);
             const T* xs = (const T*)(inb + slot * TL::kIn) + (size_t)lb * a.bs;
             if (full) enc_block_stats<T, G, true>(xs, len, vec, eb, a.omp_stats, b);
             else enc_block_stats<T, G, false>(xs, len, vec, eb, a.omp_stats, b);
@@ -414,9 +431,11 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
             if (in1) s_loc[slot][lane + 32] = i1 - sz1;
             if (lane == 0) {
                 s_agg[slot] = agg;
-                s_tile[slot] = (long long)atomicAdd(a.tile_ctr, 1ull);   // this buffer's next tile
+                const long long gn = (long long)atomicAdd(a.tile_ctr, 1ull);   // this buffer's next tile
+                s_tile[slot] = gn;
+                s_fld[slot] = (MULTI && gn < nt) ? field_of(gn) : 0;
             }
-            prefix_publish(a.st64, t, agg);
+            prefix_publish(FV(F, st_enc), t, agg);
         } else {
             // zero this tile's staging for the spliced emission
             uint4* z = (uint4*)(stgb + slot * TL::kStage);
@@ -424,28 +443,30 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         }
         __syncthreads();
         {
-            const long long tn = s_tile[slot];
-            if (tn < nt) issue(tn, slot);
+            const long long gn = s_tile[slot];
+            if (gn < nt) issue(gn, s_fld[slot], slot);
         }
         if (mine && b.state == 1) {
             uint8_t* stg = stgb + slot * TL::kStage;
             if (full) enc_block_emit<T, G, true>(stg, s_loc[slot][lb], len, b);
             else enc_block_emit<T, G, false>(stg, s_loc[slot][lb], len, b);
         }
-        if (warp == 0 && t_prev >= 0) resolve(t_prev, slot ^ 1);
+        if (warp == 0 && t_prev >= 0) resolve(fld(f_prev), t_prev, slot ^ 1);
         __syncthreads();
         if (t_prev >= 0 && !s_skip)
-            cta_copy_realign(stgb + (slot ^ 1) * TL::kStage, s_agg[slot ^ 1], a.payload + s_base);
+            cta_copy_realign(stgb + (slot ^ 1) * TL::kStage, s_agg[slot ^ 1], FV(fld(f_prev), payload) + s_base);
         t_prev = t;
+        f_prev = f;
     }
     // the last tile of this CTA: placed and written out after the loop
     if (t_prev >= 0) {
         const int ps = (i & 1) ^ 1;
-        if (warp == 0) resolve(t_prev, ps);
+        if (warp == 0) resolve(fld(f_prev), t_prev, ps);
         __syncthreads();
-        if (!s_skip) cta_copy_realign(stgb + ps * TL::kStage, s_agg[ps], a.payload + s_base);
+        if (!s_skip) cta_copy_realign(stgb + ps * TL::kStage, s_agg[ps], FV(fld(f_prev), payload) + s_base);
     }
-    if (threadIdx.x == 0 && nnc_cta) atomicAdd(&a.tot->nnc, nnc_cta);
+    if (threadIdx.x == 0 && nnc_cta) atomicAdd(&a.one.tot->nnc, nnc_cta);
+#undef FV
 }
 
 // Header, size index, state bits and medians (szx/src/szx_float.cc:1437-1483).
@@ -458,51 +479,85 @@ constexpr int kAsmThreads = 256;
 constexpr int kAsmWords = (int)(kAsmBlocksPerTile / 32);
 
 struct AsmArgs {
+    BlkField one;                // the field when nf == 1
+    const BlkField* fields;      // nf > 1: device table in ascending asm_tile0
+    int nf;
     int layout;
-    unsigned long long bs, nb;
-    uint8_t* out;
-    const Totals* tot;
-    const uint16_t* size_blk;
-    const uint32_t* med_blk;
-    const uint8_t* s_scr;
-    unsigned long long* st;      // assemble tile status, [tiles + 4]
+    unsigned long long bs;
+    unsigned long long total_tiles;
     unsigned long long* ctr;     // [0] tile counter, [1] finished CTAs
-    StreamResult* res;
-    const CodecParams* params;
-    float eb_abs;
     int* err;
 };
+
+// Header of field F (szx/src/szx_float.cc:1437-1447) and its result record.
+__device__ __forceinline__ void asm_header(const BlkField* F, int layout, unsigned long long bs, int status) {
+    const unsigned long long nb = F->nb, nnc = F->tot->nnc, nc = nb - nnc, sb = (nb + 7) / 8;
+    const bool ra = layout != kBlocked;
+    const unsigned long long hdr = ra ? 20 : 13;
+    const unsigned long long shift = ra ? 2 * nnc : 4 * nnc;
+    uint8_t* s = F->out + shift;
+    s[0] = 1; s[1] = 1; s[2] = 1; s[3] = ra ? 1 : 0;
+    if (ra) {
+        for (int k = 0; k < 8; k++) s[4 + k] = (uint8_t)(bs >> (56 - 8 * k));
+        for (int k = 0; k < 8; k++) s[12 + k] = (uint8_t)(nc >> (56 - 8 * k));
+    } else {
+        s[4] = (uint8_t)bs;
+        for (int k = 0; k < 8; k++) s[5 + k] = (uint8_t)(nc >> (56 - 8 * k));
+    }
+    StreamResult r;
+    r.offset = shift;
+    r.size = hdr + (ra ? 2 * nnc : 0) + sb + 4 * nc + F->tot->payload_bytes;
+    r.nb_const = nc;
+    r.eb = F->params ? F->params->eb : F->eb;
+    r.status = status;
+    *F->res = r;
+}
 
 __global__ void __launch_bounds__(kAsmThreads) k_blocked_assemble(AsmArgs a) {
     __shared__ uint32_t s_word[kAsmWords], s_pre[kAsmWords];
     __shared__ uint32_t s_wsum[kAsmThreads / 32];
     __shared__ long long s_t;
+    __shared__ int s_f;
     __shared__ unsigned long long s_base;
     __shared__ int s_last;
-    const unsigned long long nb = a.nb, nnc = a.tot->nnc, nc = nb - nnc, sb = (nb + 7) / 8;
-    const bool ra = a.layout != kBlocked;
-    const unsigned long long hdr = ra ? 20 : 13;
-    const unsigned long long shift = ra ? 2 * nnc : 4 * nnc;
-    uint8_t* s = a.out + shift;
-    uint8_t* O = s + hdr;
-    uint8_t* R = O + (ra ? 2 * nnc : 0);
-    uint8_t* M = R + sb;
-    const bool o_aligned = ((uintptr_t)O & 1) == 0;
-    const unsigned long long nw = (nb + 31) / 32;
-    const long long ntiles = (long long)((nw + kAsmWords - 1) / kAsmWords);
+    __shared__ BlkField s_one;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const bool ra = a.layout != kBlocked;
+    if (tid == 0 && a.nf == 1) s_one = a.one;
     for (;;) {
-        if (tid == 0) s_t = (long long)atomicAdd(a.ctr, 1ull);
+        if (tid == 0) {
+            const long long g = (long long)atomicAdd(a.ctr, 1ull);
+            int f = 0;
+            if (a.nf > 1 && g < (long long)a.total_tiles) {
+                int lo = 0, hi = a.nf - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if ((long long)a.fields[mid].asm_tile0 <= g) lo = mid;
+                    else hi = mid - 1;
+                }
+                f = lo;
+            }
+            s_t = g;
+            s_f = f;
+        }
         __syncthreads();
-        const long long t = s_t;
-        if (t >= ntiles) break;
+        if (s_t >= (long long)a.total_tiles) break;
+        const BlkField* F = a.nf == 1 ? &s_one : a.fields + s_f;
+        const long long t = s_t - (long long)F->asm_tile0;
+        const unsigned long long nb = F->nb, nnc = F->tot->nnc, sb = (nb + 7) / 8;
+        const unsigned long long hdr = ra ? 20 : 13;
+        uint8_t* O = F->out + (ra ? 2 * nnc : 4 * nnc) + hdr;
+        uint8_t* R = O + (ra ? 2 * nnc : 0);
+        uint8_t* M = R + sb;
+        const bool o_aligned = ((uintptr_t)O & 1) == 0;
+        const unsigned long long nw = (nb + 31) / 32;
         const unsigned long long w = (unsigned long long)t * kAsmWords + tid;
         uint32_t word = 0;
         if (tid < kAsmWords && w < nw) {
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const unsigned long long bi = 4 * w + j;
-                const uint32_t byte = bi < sb ? (uint32_t)a.s_scr[bi] : 0u;
+                const uint32_t byte = bi < sb ? (uint32_t)F->s_scr[bi] : 0u;
                 word = (word << 8) | byte;
                 if (bi < sb) R[bi] = (uint8_t)byte;
             }
@@ -523,8 +578,8 @@ __global__ void __launch_bounds__(kAsmThreads) k_blocked_assemble(AsmArgs a) {
             s_pre[tid] = wpre + incl - pc;
         }
         if (warp == 0) {
-            prefix_publish(a.st, t, agg);
-            const unsigned long long base = prefix_resolve(a.st, t, agg, a.err);
+            prefix_publish(F->st_asm, t, agg);
+            const unsigned long long base = prefix_resolve(F->st_asm, t, agg, a.err);
             if (lane == 0) s_base = base;
         }
         __syncthreads();
@@ -540,7 +595,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_blocked_assemble(AsmArgs a) {
             const unsigned long long rank = base + s_pre[lb >> 5] + (bit ? __popc(wd >> (32 - bit)) : 0);
             if ((wd >> (31 - bit)) & 1u) {
                 if (ra) {
-                    const uint16_t v = a.size_blk[b];
+                    const uint16_t v = F->size_blk[b];
                     if (o_aligned) {
                         *(uint16_t*)(O + 2 * rank) = v;   // little-endian u16
                     } else {
@@ -549,7 +604,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_blocked_assemble(AsmArgs a) {
                     }
                 }
             } else {
-                const uint32_t v = a.med_blk[b];
+                const uint32_t v = F->med_blk[b];
                 uint8_t* q = M + 4 * (b - rank);
                 if (a.layout == kRandomAccessNative) {
                     q[0] = (uint8_t)v; q[1] = (uint8_t)(v >> 8); q[2] = (uint8_t)(v >> 16); q[3] = (uint8_t)(v >> 24);
@@ -560,29 +615,16 @@ __global__ void __launch_bounds__(kAsmThreads) k_blocked_assemble(AsmArgs a) {
         }
         __syncthreads();
     }
-    // the last CTA to finish writes the header and the result record
+    // the last CTA to finish writes every field's header and result record
     if (tid == 0) {
         __threadfence();
         s_last = atomicAdd(&a.ctr[1], 1ull) == (unsigned long long)gridDim.x - 1;
     }
     __syncthreads();
-    if (s_last && tid == 0) {
+    if (s_last) {
         __threadfence();
-        s[0] = 1; s[1] = 1; s[2] = 1; s[3] = ra ? 1 : 0;
-        if (ra) {
-            for (int k = 0; k < 8; k++) s[4 + k] = (uint8_t)(a.bs >> (56 - 8 * k));
-            for (int k = 0; k < 8; k++) s[12 + k] = (uint8_t)(nc >> (56 - 8 * k));
-        } else {
-            s[4] = (uint8_t)a.bs;
-            for (int k = 0; k < 8; k++) s[5 + k] = (uint8_t)(nc >> (56 - 8 * k));
-        }
-        StreamResult r;
-        r.offset = shift;
-        r.size = hdr + (ra ? 2 * nnc : 0) + sb + 4 * nc + a.tot->payload_bytes;
-        r.nb_const = nc;
-        r.eb = a.params ? a.params->eb : a.eb_abs;
-        r.status = *(volatile int*)a.err;
-        *a.res = r;
+        const int status = *(volatile int*)a.err;
+        for (int f = tid; f < a.nf; f += kAsmThreads) asm_header(a.nf == 1 ? &s_one : a.fields + f, a.layout, a.bs, status);
     }
 }
 
@@ -600,49 +642,65 @@ static cudaError_t run_encode(EncArgs a, cudaStream_t s) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_blocked_encode<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             TL::kDynSmem);
+        cudaError_t e = cudaFuncSetAttribute(k_blocked_encode<T, G, false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, TL::kDynSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_blocked_encode<T, G, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     TL::kDynSmem);
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
-    a.ntiles = (a.nb + TL::kBlocks - 1) / TL::kBlocks;
     const size_t g = (size_t)sm_count() * 3;
-    const int grid = (int)(a.ntiles < g ? a.ntiles : g);
+    const int grid = (int)(a.total_tiles < g ? a.total_tiles : g);
     TraceScope tr("blocked_encode", s);
-    k_blocked_encode<T, G><<<grid, kEncThreads, TL::kDynSmem, s>>>(a);
+    if (a.nf > 1) k_blocked_encode<T, G, true><<<grid, kEncThreads, TL::kDynSmem, s>>>(a);
+    else k_blocked_encode<T, G, false><<<grid, kEncThreads, TL::kDynSmem, s>>>(a);
     return cudaGetLastError();
 }
 
-
-cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
-                                  float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s) {
-    if (n == 0 || bs < 1 || bs > 256) return cudaErrorInvalidValue;
-    if (layout == kBlocked && bs > 255) return cudaErrorInvalidValue;
-    const size_t nb = (n + bs - 1) / bs, sb = (nb + 7) / 8;
-    const size_t hdr = layout == kBlocked ? 13 : 20;
-    const size_t qfix = hdr + sb + 4 * nb;
-    if (cap < qfix) return cudaErrorInvalidValue;
-    unsigned long long* st_enc = ws.st_word;
-    unsigned long long* st_asm = ws.st_word + enc_status_words(nb);   // encoder's words first
-    cudaError_t e;
-    // status words of both look-backs, then totals / result / error / counters
-    if ((e = cudaMemsetAsync(ws.st_word, 0, 8 * blocked_status_words(nb), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync((uint8_t*)ws.totals, 0, kWsHeaderClear, s)) != cudaSuccess) return e;
-    EncArgs a;
-    a.st64 = st_enc;
-    a.x = x; a.n = n; a.nb = nb; a.ntiles = 0; a.bs = bs; a.eb = abs_eb;
-    a.omp_stats = layout == kRandomAccessNative;
-    a.params = use_params ? ws.params : nullptr;
-    a.payload = d_out + qfix;
-    a.payload_cap = cap - qfix;
-    a.size_blk = ws.o_scr; a.med_blk = ws.m_scr; a.s_scr = ws.s_scr;
-    a.tile_ctr = &ws.counters[0];
-    a.err = ws.err;
-    a.tot = ws.totals;
-    // lanes per block: values per lane are 16 (float) / 8 (double)
-    const int per = dtype == 0 ? 16 : 8;
+static int lanes_for_bs(int dtype, int bs) {
+    const int per = dtype == 0 ? 16 : 8;   // values per lane
     const int need = (bs + per - 1) / per;
-    const int G = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
+    return need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
+}
+
+int blocked_tile_blocks(int dtype, int bs) {
+    const int G = lanes_for_bs(dtype, bs);
+    if (dtype == 0) {
+        switch (G) {
+            case 1: return EncTile<float, 1>::kBlocks;
+            case 2: return EncTile<float, 2>::kBlocks;
+            case 4: return EncTile<float, 4>::kBlocks;
+            case 8: return EncTile<float, 8>::kBlocks;
+            default: return EncTile<float, 16>::kBlocks;
+        }
+    }
+    switch (G) {
+        case 1: return EncTile<double, 1>::kBlocks;
+        case 2: return EncTile<double, 2>::kBlocks;
+        case 4: return EncTile<double, 4>::kBlocks;
+        case 8: return EncTile<double, 8>::kBlocks;
+        case 16: return EncTile<double, 16>::kBlocks;
+        default: return EncTile<double, 32>::kBlocks;
+    }
+}
+
+cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, const BlkField& one,
+                                         const BlkField* d_fields, unsigned long long enc_total,
+                                         unsigned long long asm_total, unsigned long long* counters, int* err,
+                                         cudaStream_t s) {
+    if (nf < 1 || enc_total == 0) return cudaErrorInvalidValue;
+    EncArgs a;
+    a.one = one;
+    a.fields = d_fields;
+    a.nf = nf;
+    a.bs = bs;
+    a.omp_stats = layout == kRandomAccessNative;
+    a.total_tiles = enc_total;
+    a.tile_ctr = &counters[0];
+    a.err = err;
+    cudaError_t e;
+    const int G = lanes_for_bs(dtype, bs);
     if (dtype == 0) {
         switch (G) {
             case 1: e = run_encode<float, 1>(a, s); break;
@@ -663,16 +721,50 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
     }
     if (e != cudaSuccess) return e;
     AsmArgs m;
-    m.layout = layout; m.bs = (unsigned long long)bs; m.nb = nb; m.out = d_out; m.tot = ws.totals;
-    m.size_blk = ws.o_scr; m.med_blk = ws.m_scr; m.s_scr = ws.s_scr;
-    m.st = st_asm; m.ctr = &ws.counters[1]; m.res = ws.result;
-    m.params = use_params ? ws.params : nullptr; m.eb_abs = abs_eb; m.err = ws.err;
-    const size_t tiles = (nb + 32 * kAsmWords - 1) / (32 * kAsmWords);
+    m.one = one;
+    m.fields = d_fields;
+    m.nf = nf;
+    m.layout = layout;
+    m.bs = (unsigned long long)bs;
+    m.total_tiles = asm_total;
+    m.ctr = &counters[1];
+    m.err = err;
     const size_t gmax = (size_t)sm_count() * 4;
-    const int ag = (int)(tiles < gmax ? tiles : gmax);
+    const int ag = (int)(asm_total < gmax ? (asm_total ? asm_total : 1) : gmax);
     TraceScope tr("blocked_assemble", s);
     k_blocked_assemble<<<ag, kAsmThreads, 0, s>>>(m);
     return cudaGetLastError();
+}
+
+cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
+                                  float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s) {
+    if (n == 0 || bs < 1 || bs > 256) return cudaErrorInvalidValue;
+    if (layout == kBlocked && bs > 255) return cudaErrorInvalidValue;
+    const size_t nb = (n + bs - 1) / bs, sb = (nb + 7) / 8;
+    const size_t hdr = layout == kBlocked ? 13 : 20;
+    const size_t qfix = hdr + sb + 4 * nb;
+    if (cap < qfix) return cudaErrorInvalidValue;
+    cudaError_t e;
+    // status words of both look-backs, then totals / result / error / counters
+    if ((e = cudaMemsetAsync(ws.st_word, 0, 8 * blocked_status_words(nb), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync((uint8_t*)ws.totals, 0, kWsHeaderClear, s)) != cudaSuccess) return e;
+    const size_t tb = (size_t)blocked_tile_blocks(dtype, bs);
+    BlkField F;
+    F.x = x; F.n = n; F.nb = nb;
+    F.enc_tiles = (nb + tb - 1) / tb; F.enc_tile0 = 0;
+    F.asm_tiles = (nb + kAsmBlocksPerTile - 1) / kAsmBlocksPerTile; F.asm_tile0 = 0;
+    F.eb = abs_eb; F.pad = 0;
+    F.params = use_params ? ws.params : nullptr;
+    F.out = d_out;
+    F.payload = d_out + qfix;
+    F.payload_cap = cap - qfix;
+    F.st_enc = ws.st_word;
+    F.st_asm = ws.st_word + enc_status_words(nb);   // encoder's words first
+    F.size_blk = ws.o_scr; F.med_blk = ws.m_scr; F.s_scr = ws.s_scr;
+    F.tot = ws.totals;
+    F.res = ws.result;
+    return launch_blocked_encode_fields(layout, dtype, bs, 1, F, nullptr, F.enc_tiles, F.asm_tiles, ws.counters,
+                                        ws.err, s);
 }
 
 // ------------------------------------------------------------------ decode

@@ -53,6 +53,31 @@ struct NonBlockedHdr {
 
 enum Layout : int { kNonBlocked = 1, kBlocked = 2, kRandomAccess = 3, kRandomAccessNative = 4 };
 
+// Sets what SZxG_get_last_error() reports on this host thread (api.cu).
+void set_last_error(int e);
+
+// One field of a blocked-layout encode launch (a single-field call is a
+// table of one): where its values, stream and scratch live.
+struct BlkField {
+    const void* x;                               // values (device)
+    unsigned long long n, nb;                    // values, blocks
+    unsigned long long enc_tiles, enc_tile0;     // encode tiles, first launch-wide encode tile
+    unsigned long long asm_tiles, asm_tile0;     // assemble tiles, first launch-wide assemble tile
+    float eb;                                    // absolute bound (params->eb when params is set)
+    int pad;
+    const CodecParams* params;
+    uint8_t* out;                                // stream buffer; the stream lands at out + res->offset
+    uint8_t* payload;                            // fixed payload position (out + header, index, medians)
+    unsigned long long payload_cap;
+    unsigned long long* st_enc;                  // encode look-back status [enc_tiles + 4], zeroed
+    unsigned long long* st_asm;                  // assemble look-back status [asm_tiles + 4], zeroed
+    uint16_t* size_blk;                          // [nb] payload bytes by block
+    uint32_t* med_blk;                           // [nb] stored medians by block
+    uint8_t* s_scr;                              // state bits [nb / 8 + 64]
+    Totals* tot;                                 // zeroed
+    StreamResult* res;
+};
+
 // ------------------------------------------------------------------ workspace
 
 // Device scratch needed by one compress or decompress call; carved by
@@ -147,6 +172,16 @@ cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float
 size_t blocked_bound(int layout, int dtype, size_t n, int bs);
 cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
                                   float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s);
+// Blocks per encode tile for this type and block size (tile counts of a
+// field table), and the encode + assemble of nf fields in one launch each:
+// `one` when nf == 1, else the device table d_fields (ascending tile starts);
+// counters[0..2] and err zeroed by the caller, like every field's status
+// words and totals.
+int blocked_tile_blocks(int dtype, int bs);
+cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, const BlkField& one,
+                                         const BlkField* d_fields, unsigned long long enc_total,
+                                         unsigned long long asm_total, unsigned long long* counters, int* err,
+                                         cudaStream_t s);
 // Blocked decode (layouts 3, 4).
 cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream, size_t len, size_t n, int bs,
                                   void* d_out, const Workspace& ws, cudaStream_t s);

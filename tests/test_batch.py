@@ -1,0 +1,144 @@
+"""Batched fields: one persistent launch per kernel over a work queue of
+(field, block-range) tiles.  Every field's stream must equal what the
+single-field entry point produces for it (which the parity tests pin to the
+reference), for uneven sizes down to one value, and replaying the batch from
+a captured CUDA graph must reproduce it.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+class Field(C.Structure):
+    _fields_ = [("in_", C.c_void_p), ("nbEle", C.c_size_t), ("inBytes", C.c_size_t), ("absErrBound", C.c_float),
+                ("reserved", C.c_int), ("out", C.c_void_p), ("outCapacity", C.c_size_t)]
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("a CUDA device is required")
+    from szx_gb300 import build
+    build.build()
+    from szx_gb300._lib import StreamInfo, lib
+    L = lib()
+    L.SZxG_batch_create.restype = C.c_void_p
+    L.SZxG_batch_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    L.SZxG_batch_run.restype = C.c_int
+    L.SZxG_batch_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.SZxG_batch_status.restype = C.c_int
+    L.SZxG_batch_status.argtypes = [C.c_void_p, C.c_void_p]
+    L.SZxG_batch_destroy.restype = None
+    L.SZxG_batch_destroy.argtypes = [C.c_void_p]
+    return torch, L, StreamInfo
+
+
+def _single(env, mode, x, bs, eb):
+    torch, L, StreamInfo = env
+    code = 0 if x.dtype == torch.float32 else 1
+    n = x.numel()
+    cap = L.SZxG_compress_bound(mode, code, n, bs)
+    wsb = L.SZxG_workspace_size(mode, code, n, bs)
+    out = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    ws = torch.zeros(wsb, dtype=torch.uint8, device="cuda")
+    info = torch.zeros(C.sizeof(StreamInfo), dtype=torch.uint8, device="cuda")
+    rc = L.SZxG_compress(mode, code, C.c_void_p(x.data_ptr()), n, bs, 0, eb, 0.0, C.c_void_p(out.data_ptr()), cap,
+                         C.c_void_p(ws.data_ptr()), wsb, C.c_void_p(info.data_ptr()),
+                         C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0
+    i = StreamInfo.from_buffer_copy(info.cpu().numpy().tobytes())
+    return out[i.offset: i.offset + i.size].cpu().numpy().tobytes()
+
+
+def _batch(env, mode, xs, bs, ebs, graph=False):
+    torch, L, StreamInfo = env
+    code = 0 if xs[0].dtype == torch.float32 else 1
+    outs, fields = [], (Field * len(xs))()
+    for k, (x, eb) in enumerate(zip(xs, ebs)):
+        cap = L.SZxG_compress_bound(mode, code, x.numel(), bs)
+        o = torch.empty(cap, dtype=torch.uint8, device="cuda")
+        outs.append(o)
+        fields[k] = Field(x.data_ptr(), x.numel(), 0, eb, 0, o.data_ptr(), cap)
+    b = L.SZxG_batch_create(0, mode, code, bs, len(xs), C.cast(fields, C.c_void_p))
+    assert b, L.SZxG_error_string(L.SZxG_get_last_error())
+    info = torch.zeros(len(xs) * C.sizeof(StreamInfo), dtype=torch.uint8, device="cuda")
+    try:
+        if graph:
+            g = torch.cuda.CUDAGraph()
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                assert L.SZxG_batch_run(b, C.c_void_p(info.data_ptr()), C.c_void_p(s.cuda_stream)) == 0   # warm
+            torch.cuda.current_stream().wait_stream(s)
+            torch.cuda.synchronize()
+            for o in outs:
+                o.zero_()
+            info.zero_()
+            with torch.cuda.graph(g):
+                rc = L.SZxG_batch_run(b, C.c_void_p(info.data_ptr()),
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream))
+                assert rc == 0
+            torch.cuda.synchronize()
+            for o in outs:
+                o.zero_()
+            g.replay()
+            g.replay()
+        else:
+            assert L.SZxG_batch_run(b, C.c_void_p(info.data_ptr()),
+                                    C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+        assert L.SZxG_batch_status(b, C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+        torch.cuda.synchronize()
+        raw = info.cpu().numpy().tobytes()
+        res = []
+        for k, o in enumerate(outs):
+            i = StreamInfo.from_buffer_copy(raw[k * C.sizeof(StreamInfo):(k + 1) * C.sizeof(StreamInfo)])
+            assert i.status == 0
+            res.append(o[i.offset: i.offset + i.size].cpu().numpy().tobytes())
+        return res
+    finally:
+        L.SZxG_batch_destroy(b)
+
+
+def _fields(torch, dt, sizes, seed):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    xs, ebs = [], []
+    for k, n in enumerate(sizes):
+        kind = k % 3
+        if kind == 0:      # smooth random walk
+            x = torch.randn(n, generator=g, device="cuda", dtype=torch.float64).cumsum(0) * 1e-2
+        elif kind == 1:    # piecewise constant
+            x = torch.repeat_interleave(torch.randn(n // 300 + 1, generator=g, device="cuda",
+                                                    dtype=torch.float64), 300)[:n]
+        else:              # white noise
+            x = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
+        x = x.to(dt).contiguous()
+        rng = float((x.max() - x.min()).item()) or 1.0
+        ebs.append(float(np.float32(rng * 10 ** (-2 - 3 * ((k * 7919) % 97) / 96.0))))
+        xs.append(x)
+    return xs, ebs
+
+
+@pytest.mark.parametrize("mode,dtname,bs", [(3, "float32", 128), (4, "float64", 64), (2, "float32", 128),
+                                            (3, "float64", 256)])
+def test_batch_streams_equal_single_field_streams(env, mode, dtname, bs):
+    torch = env[0]
+    dt = getattr(torch, dtname)
+    rng = np.random.default_rng(5)
+    sizes = [1, 2, 127, 128, 129, 4097, 65536] + [int(v) for v in np.exp(rng.uniform(np.log(1 << 14),
+                                                                                       np.log(1 << 21), 40))]
+    xs, ebs = _fields(torch, dt, sizes, 7)
+    got = _batch(env, mode, xs, bs, ebs)
+    for k, (x, eb) in enumerate(zip(xs, ebs)):
+        assert got[k] == _single(env, mode, x, bs, eb), (k, x.numel())
+
+
+def test_batch_replays_from_a_cuda_graph(env):
+    torch = env[0]
+    xs, ebs = _fields(torch, torch.float32, [5000, 1 << 20, 333, 1 << 18, 70001], 11)
+    want = _batch(env, 3, xs, 128, ebs)
+    got = _batch(env, 3, xs, 128, ebs, graph=True)
+    assert got == want
