@@ -46,6 +46,10 @@ WORKLOADS = {
                      "(profiling size: 216 MiB, above L2)"),
     "c2m1": dict(shape=(512, 512, 512), mode=1, bs=128, rel=1e-3,
                  desc="512^3 float32 k^-5/3 Gaussian random field + 5% zero slabs, REL 1e-3, fastMode 1"),
+    "c4": dict(mode=3, bs=128,
+               desc="batched: float32 fields, sizes log-uniform 2^14..2^26, seeded mix of spectral / "
+                    "piecewise-constant / white noise, per-field ABS bound log-uniform 1e-5..1e-2 x range, "
+                    "fastMode 3, blockSize 128"),
 }
 
 
@@ -332,6 +336,154 @@ def run_ours(args, wl, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def make_batch_fields(nf, seed, device):
+    """C4 fields on the device: sizes log-uniform 2^14..2^26, each a seeded
+    1-D spectral field (k^-5/3), piecewise-constant levels or white noise,
+    with an ABS bound log-uniform in 1e-5..1e-2 of its range."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(2 ** 14), np.log(2 ** 26), nf)).astype(np.int64)
+    kinds = rng.integers(0, 3, nf)
+    scales = 10.0 ** rng.uniform(-5, -2, nf)
+    g = torch.Generator(device=device).manual_seed(seed)
+    xs, ebs = [], []
+    for n, kind, sc in zip(sizes, kinds, scales):
+        n = int(n)
+        if kind == 0:   # synthesised at the next power of two, then truncated
+            n2 = 1 << (n - 1).bit_length()
+            nf_ = n2 // 2 + 1
+            k = torch.arange(nf_, device=device, dtype=torch.float32)
+            k[0] = 1.0
+            amp = k ** (-5.0 / 6.0)
+            amp[0] = 0.0
+            z = torch.complex(torch.randn(nf_, generator=g, device=device),
+                              torch.randn(nf_, generator=g, device=device)) * amp
+            x = torch.fft.irfft(z, n=n2)[:n]
+            x = (x - x.mean()) / (x.std() + 1e-30)
+        elif kind == 1:
+            run = int(rng.integers(64, 4096))
+            x = torch.repeat_interleave(torch.randn(n // run + 1, generator=g, device=device), run)[:n].contiguous()
+        else:
+            x = torch.randn(n, generator=g, device=device)
+        x = x.float().contiguous()
+        r = float((x.max() - x.min()).item()) or 1.0
+        xs.append(x)
+        ebs.append(float(r * sc))
+    return xs, ebs
+
+
+def run_batched(args, wl):
+    """C4: one batch (one persistent launch per kernel, replayed from a CUDA
+    graph) against the same fields compressed by per-field calls."""
+    import numpy as np
+    import torch
+
+    from szx_gb300._lib import StreamInfo, lib
+
+    class Field(C.Structure):
+        _fields_ = [("in_", C.c_void_p), ("nbEle", C.c_size_t), ("inBytes", C.c_size_t),
+                    ("absErrBound", C.c_float), ("reserved", C.c_int), ("out", C.c_void_p), ("outCapacity", C.c_size_t)]
+
+    L = lib()
+    L.SZxG_batch_create.restype = C.c_void_p
+    L.SZxG_batch_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    L.SZxG_batch_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.SZxG_batch_status.argtypes = [C.c_void_p, C.c_void_p]
+    L.SZxG_batch_destroy.argtypes = [C.c_void_p]
+    mode, bs = wl["mode"], wl["bs"]
+    xs, ebs = make_batch_fields(args.fields, 4242, "cuda")
+    nf = len(xs)
+    total_in = sum(x.numel() for x in xs) * 4
+    outs, fields = [], (Field * nf)()
+    for k, (x, eb) in enumerate(zip(xs, ebs)):
+        cap = L.SZxG_compress_bound(mode, 0, x.numel(), bs)
+        o = torch.empty(cap, dtype=torch.uint8, device="cuda")
+        outs.append(o)
+        fields[k] = Field(x.data_ptr(), x.numel(), 0, eb, 0, o.data_ptr(), cap)
+    b = L.SZxG_batch_create(0, mode, 0, bs, nf, C.cast(fields, C.c_void_p))
+    assert b, L.SZxG_error_string(L.SZxG_get_last_error())
+    info = torch.zeros(nf * C.sizeof(StreamInfo), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(args.warmup):
+            assert L.SZxG_batch_run(b, C.c_void_p(info.data_ptr()), C.c_void_p(s.cuda_stream)) == 0
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        assert L.SZxG_batch_run(b, C.c_void_p(info.data_ptr()), C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+    graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    time.sleep(0.3)
+    e0.record()
+    for _ in range(args.steps):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    batched_ms = e0.elapsed_time(e1) / args.steps
+    assert L.SZxG_batch_status(b, C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+    raw = info.cpu().numpy().tobytes()
+    sizes_out = [StreamInfo.from_buffer_copy(raw[k * C.sizeof(StreamInfo):(k + 1) * C.sizeof(StreamInfo)]).size
+                 for k in range(nf)]
+    # per-field launches of the same fields (one reused workspace)
+    wsb = max(L.SZxG_workspace_size(mode, 0, x.numel(), bs) for x in xs)
+    ws = torch.zeros(wsb, dtype=torch.uint8, device="cuda")
+    inf1 = torch.zeros(C.sizeof(StreamInfo), dtype=torch.uint8, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def one(k):
+        x = xs[k]
+        return L.SZxG_compress(mode, 0, C.c_void_p(x.data_ptr()), x.numel(), bs, 0, ebs[k], 0.0,
+                               C.c_void_p(outs[k].data_ptr()), outs[k].numel(), C.c_void_p(ws.data_ptr()), wsb,
+                               C.c_void_p(inf1.data_ptr()), st)
+    for k in range(nf):
+        assert one(k) == 0
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(nf + 1)]
+    per_field = []
+    loop_ms = []
+    for _ in range(max(1, args.steps // 2)):
+        evs[0].record()
+        for k in range(nf):
+            one(k)
+            evs[k + 1].record()
+        torch.cuda.synchronize()
+        loop_ms.append(evs[0].elapsed_time(evs[nf]))
+        per_field = [evs[k].elapsed_time(evs[k + 1]) for k in range(nf)]
+    loop_ms = statistics.median(loop_ms)
+    # one large field alone (the single-field reference point for the batch)
+    big = max(range(nf), key=lambda k: xs[k].numel())
+    e0.record()
+    for _ in range(args.steps):
+        one(big)
+    e1.record()
+    torch.cuda.synchronize()
+    big_gbs = xs[big].numel() * 4 / (e0.elapsed_time(e1) / args.steps / 1000) / 1e9
+    L.SZxG_batch_destroy(b)
+    pf = np.array(per_field)
+    line = {
+        "metric": "batched compress GB/s (mixed float32 fields, ABS)", "value": round(total_in / (batched_ms / 1000) / 1e9, 2),
+        "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(batched_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded on-device fields)",
+        "config": {"workload": wl["desc"], "fields": nf, "elements": total_in // 4,
+                   "stream_bytes": int(sum(sizes_out)), "graph": True,
+                   "l2": "total input far above L2; no flush needed"},
+        "per_field_launches": {"value": round(total_in / (loop_ms / 1000) / 1e9, 2), "unit": "GB/s",
+                               "ms_per_step": round(loop_ms, 3), "p50_ms": round(float(np.percentile(pf, 50)), 4),
+                               "p99_ms": round(float(np.percentile(pf, 99)), 4)},
+        "single_field_gbs": round(big_gbs, 2), "single_field_elements": xs[big].numel(),
+        "batched_vs_single": round(total_in / (batched_ms / 1000) / 1e9 / big_gbs, 3),
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -339,6 +491,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--fields", type=int, default=2000, help="c4: number of fields")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -347,6 +500,9 @@ def main():
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl, rank, world)
+        return
+    if args.workload == "c4":
+        run_batched(args, wl)
         return
     if world > 1:
         import torch
