@@ -466,6 +466,58 @@ def run_batched(args, wl):
     big_gbs = xs[big].numel() * 4 / (e0.elapsed_time(e1) / args.steps / 1000) / 1e9
     L.SZxG_batch_destroy(b)
     pf = np.array(per_field)
+
+    # the same streams decoded as one batch (graph replay) and by per-field calls
+    offs = [StreamInfo.from_buffer_copy(raw[k * C.sizeof(StreamInfo):(k + 1) * C.sizeof(StreamInfo)]).offset
+            for k in range(nf)]
+    ys, dfields = [], (Field * nf)()
+    for k in range(nf):
+        y = torch.empty_like(xs[k])
+        ys.append(y)
+        dfields[k] = Field(outs[k].data_ptr() + offs[k], xs[k].numel(), sizes_out[k], 0.0, 0, y.data_ptr(),
+                           y.numel() * 4)
+    bd = L.SZxG_batch_create(1, mode, 0, bs, nf, C.cast(dfields, C.c_void_p))
+    assert bd, L.SZxG_error_string(L.SZxG_get_last_error())
+    dinfo = torch.zeros(nf * C.sizeof(StreamInfo), dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(s):
+        for _ in range(args.warmup):
+            assert L.SZxG_batch_run(bd, C.c_void_p(dinfo.data_ptr()), C.c_void_p(s.cuda_stream)) == 0
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    dgraph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(dgraph):
+        assert L.SZxG_batch_run(bd, C.c_void_p(dinfo.data_ptr()),
+                                C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+    dgraph.replay()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        dgraph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    dec_ms = e0.elapsed_time(e1) / args.steps
+    dec_status = L.SZxG_batch_status(bd, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    L.SZxG_batch_destroy(bd)
+    assert dec_status == 0, dec_status
+    bad = sum(int(not bool((ys[k] - xs[k]).abs().max() <= ebs[k] * 1.001)) for k in range(nf))
+
+    def one_dec(k):
+        return L.SZxG_decompress(mode, 0, C.c_void_p(outs[k].data_ptr() + offs[k]), sizes_out[k], xs[k].numel(), bs,
+                                 C.c_void_p(ys[k].data_ptr()), C.c_void_p(ws.data_ptr()), wsb, st)
+    for k in range(nf):
+        assert one_dec(k) == 0
+    torch.cuda.synchronize()
+    dloop = []
+    for _ in range(max(1, args.steps // 2)):
+        evs[0].record()
+        for k in range(nf):
+            one_dec(k)
+            evs[k + 1].record()
+        torch.cuda.synchronize()
+        dloop.append(evs[0].elapsed_time(evs[nf]))
+        dper = [evs[k].elapsed_time(evs[k + 1]) for k in range(nf)]
+    dloop = statistics.median(dloop)
+    dpf = np.array(dper)
     line = {
         "metric": "batched compress GB/s (mixed float32 fields, ABS)", "value": round(total_in / (batched_ms / 1000) / 1e9, 2),
         "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(batched_ms, 4),
@@ -479,6 +531,11 @@ def run_batched(args, wl):
                                "p99_ms": round(float(np.percentile(pf, 99)), 4)},
         "single_field_gbs": round(big_gbs, 2), "single_field_elements": xs[big].numel(),
         "batched_vs_single": round(total_in / (batched_ms / 1000) / 1e9 / big_gbs, 3),
+        "decompress": {"batched_gbs": round(total_in / (dec_ms / 1000) / 1e9, 2), "ms_per_step": round(dec_ms, 4),
+                       "per_field_gbs": round(total_in / (dloop / 1000) / 1e9, 2),
+                       "p50_ms": round(float(np.percentile(dpf, 50)), 4),
+                       "p99_ms": round(float(np.percentile(dpf, 99)), 4),
+                       "fields_over_bound": bad},
         "clocks": clk,
     }
     print(json.dumps(line))

@@ -203,8 +203,11 @@ typedef struct SZxG_Batch SZxG_Batch;
  * Returns NULL on failure (SZxG_get_last_error). */
 SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blockSize, int nFields,
                               const SZxG_Field* fields);
-/* Enqueue the batch; compress results (stream at out + offset) go to
- * d_info[nFields] when d_info is not NULL. */
+/* Enqueue the batch; per-field results go to d_info[nFields] when d_info is
+ * not NULL: compress, where the stream sits (out + offset, size bytes);
+ * decompress, the field's status (a malformed stream fails only its own
+ * field, whose values are then unspecified) and size = nbEle * element size.
+ * Each decompress stream's blockSize must equal the batch's. */
 int SZxG_batch_run(SZxG_Batch* batch, SZxG_StreamInfo* d_info, void* stream);
 /* Wait for `stream` and report the batch's error word (0: all fields fine). */
 int SZxG_batch_status(SZxG_Batch* batch, void* stream);

@@ -1,5 +1,8 @@
 // Batches: many fields of one type and block size coded by one persistent
 // launch per kernel over a device work queue of (field, block-range) tiles.
+// Compress (direction 0): fastMode 2, 3, 4.  Decompress (direction 1):
+// fastMode 3 and 4, whose size index makes every stream's payload offsets a
+// scan; a fastMode-2 stream needs the single-stream boundary search.
 //
 // The blocked kernels take a table of fields (a single-field call is a table
 // of one): a launch-wide tile index maps to (field, local tile) by a binary
@@ -31,6 +34,8 @@ struct SZxG_Batch {
     uint8_t* zero = nullptr;          // status words and totals of every field
     size_t zero_bytes = 0;
     unsigned long long enc_total = 0, asm_total = 0;
+    DecField* d_dec = nullptr;        // decode: device table
+    unsigned long long idx_total = 0, dec_total = 0;
 };
 
 namespace {
@@ -46,9 +51,87 @@ SZxG_Batch* fail(int code) {
 
 extern "C" {
 
+static SZxG_Batch* create_decode(int fastMode, int dataType, int blockSize, int nFields, const SZxG_Field* fields) {
+    if (fastMode != kRandomAccess && fastMode != kRandomAccessNative) return fail(SZXG_ERR_UNSUPPORTED);
+    if (blockSize < 1 || blockSize > 256) return fail(SZXG_ERR_ARG);
+    const size_t nf = (size_t)nFields, es = dataType == 0 ? 4 : 8;
+    const size_t tb = (size_t)blocked_dec_tile_blocks(dataType, blockSize);
+    // layout: table | results | counters+err | headers | zeroed (errors, look-back words) | offsets, ranks
+    size_t off = 0;
+    const size_t o_tab = off; off += a256(sizeof(DecField) * nf);
+    const size_t o_res = off; off += a256(sizeof(StreamResult) * nf);
+    const size_t o_ctr = off; off += 256;
+    const size_t o_hdr = off; off += a256(sizeof(BlockedHdr) * nf);
+    const size_t o_zero = off;
+    const size_t o_err = off; off += a256(sizeof(int) * nf);
+    std::vector<size_t> o_st(nf), o_p(nf), o_rw(nf), ta(nf), tbw(nf);
+    for (size_t f = 0; f < nf; f++) {
+        const SZxG_Field& F = fields[f];
+        if (!F.in || !F.out || F.nbEle == 0) return fail(SZXG_ERR_ARG);
+        if (F.outCapacity < F.nbEle * es) return fail(SZXG_ERR_CAPACITY);
+        const size_t nb = (F.nbEle + blockSize - 1) / blockSize, nw = (nb + 31) / 32;
+        ta[f] = (nb + kIdxPerTile - 1) / kIdxPerTile;
+        tbw[f] = (nw + kIdxPerTile - 1) / kIdxPerTile;
+        o_st[f] = off; off += a256(3 * 8 * (ta[f] + tbw[f]));
+    }
+    const size_t zero_bytes = off - o_zero;
+    for (size_t f = 0; f < nf; f++) {
+        const size_t nb = (fields[f].nbEle + blockSize - 1) / blockSize;
+        o_p[f] = off; off += a256(8 * (nb + 1));
+        o_rw[f] = off; off += a256(4 * (nb / 32 + 2));
+    }
+    SZxG_Batch* b = new SZxG_Batch();
+    b->direction = 1; b->mode = fastMode; b->dtype = dataType; b->bs = blockSize; b->nf = nFields;
+    if (cudaMalloc(&b->dev, off) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return fail(SZXG_ERR_CUDA);
+    }
+    uint8_t* base = (uint8_t*)b->dev;
+    b->results = (StreamResult*)(base + o_res);
+    b->counters = (unsigned long long*)(base + o_ctr);
+    b->err = (int*)(base + o_ctr + 64);
+    b->zero = base + o_zero;
+    b->zero_bytes = zero_bytes;
+    std::vector<DecField> tab(nf);
+    unsigned long long it = 0, dt = 0;
+    for (size_t f = 0; f < nf; f++) {
+        const SZxG_Field& S = fields[f];
+        DecField& D = tab[f];
+        memset(&D, 0, sizeof D);
+        D.s = (const uint8_t*)S.in; D.len = S.inBytes; D.n = S.nbEle;
+        D.nb = (S.nbEle + blockSize - 1) / blockSize;
+        D.out = S.out;
+        D.hdr = (BlockedHdr*)(base + o_hdr) + f;
+        D.P = (unsigned long long*)(base + o_p[f]);
+        D.RW = (uint32_t*)(base + o_rw[f]);
+        unsigned long long* st = (unsigned long long*)(base + o_st[f]);
+        for (int k = 0; k < 3; k++) D.stA[k] = st + k * ta[f];
+        st += 3 * ta[f];
+        for (int k = 0; k < 3; k++) D.stB[k] = st + k * tbw[f];
+        D.idxA_tiles = ta[f]; D.idxB_tiles = tbw[f];
+        D.idx_tile0 = it; it += ta[f] + tbw[f];
+        D.dec_tiles = (D.nb + tb - 1) / tb;
+        D.dec_tile0 = dt; dt += D.dec_tiles;
+        D.err = (int*)(base + o_err) + f;
+    }
+    b->idx_total = it;
+    b->dec_total = dt;
+    b->d_dec = (DecField*)(base + o_tab);
+    if (cudaMemcpy(b->d_dec, tab.data(), sizeof(DecField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(b->dev);
+        delete b;
+        return fail(SZXG_ERR_CUDA);
+    }
+    set_last_error(SZXG_OK);
+    return b;
+}
+
 SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blockSize, int nFields,
                               const SZxG_Field* fields) {
-    if (direction == 1) return fail(SZXG_ERR_UNSUPPORTED);
+    if (direction == 1 && nFields >= 1 && fields && (dataType == 0 || dataType == 1))
+        return create_decode(fastMode, dataType, blockSize, nFields, fields);
     if (direction != 0 || nFields < 1 || !fields || (dataType != 0 && dataType != 1)) return fail(SZXG_ERR_ARG);
     if (fastMode != kBlocked && fastMode != kRandomAccess && fastMode != kRandomAccessNative)
         return fail(SZXG_ERR_UNSUPPORTED);
@@ -135,7 +218,10 @@ int SZxG_batch_run(SZxG_Batch* b, SZxG_StreamInfo* d_info, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemsetAsync(b->zero, 0, b->zero_bytes, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->counters, 0, 128, s);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && b->direction == 1)
+        e = launch_blocked_decode_fields(b->mode, b->dtype, b->bs, b->nf, b->d_dec, b->idx_total, b->dec_total,
+                                         b->counters, b->results, b->err, s);
+    else if (e == cudaSuccess)
         e = launch_blocked_encode_fields(b->mode, b->dtype, b->bs, b->nf, b->one, b->nf > 1 ? b->d_fields : nullptr,
                                          b->enc_total, b->asm_total, b->counters, b->err, s);
     if (e == cudaSuccess && d_info)

@@ -776,8 +776,8 @@ __device__ __forceinline__ unsigned long long be64(const uint8_t* p) {
 }
 
 // Parse and validate the mode-3/4 header (szx/src/szxd_float.cc:402-434).
-__global__ void k_blocked_parse(const uint8_t* s, unsigned long long len, unsigned long long n,
-                                unsigned long long bs_expect, BlockedHdr* h, int* err) {
+__device__ BlockedHdr parse_blocked(const uint8_t* s, unsigned long long len, unsigned long long n,
+                                    unsigned long long bs_expect) {
     BlockedHdr r = {};
     r.n = n;
     r.ok = 0;
@@ -797,8 +797,24 @@ __global__ void k_blocked_parse(const uint8_t* s, unsigned long long len, unsign
             }
         }
     }
+    return r;
+}
+
+__global__ void k_blocked_parse(const uint8_t* s, unsigned long long len, unsigned long long n,
+                                unsigned long long bs_expect, BlockedHdr* h, int* err) {
+    const BlockedHdr r = parse_blocked(s, len, n, bs_expect);
     *h = r;
     *err = r.ok ? kErrNone : kErrStream;
+}
+
+// Every stream of a batch: one thread per field.
+__global__ void k_blocked_parse_fields(const DecField* F, int nf, unsigned long long bs) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const DecField& D = F[f];
+    const BlockedHdr r = parse_blocked(D.s, D.len, D.n, bs);
+    *D.hdr = r;
+    if (!r.ok) *D.err = kErrStream;
 }
 
 // CTA-wide exclusive sum over kIdxThreads threads.
@@ -820,9 +836,62 @@ __device__ __forceinline__ unsigned long long cta_exclusive_sum(unsigned long lo
     return wpre + incl - v;
 }
 
-// Two independent exclusive scans in one persistent launch:
+// Two independent exclusive scans:
 //   family A: payload offsets  P[k] = sum O[0..k)          (k < nnc)
 //   family B: rank words       RW[w] = popcount(state < 32w) (w < ceil(nb/32))
+// One tile (kIdxPerTile items) of either, by the whole CTA.
+__device__ __forceinline__ void index_tile(const uint8_t* s, const BlockedHdr& h, unsigned long long* P, uint32_t* RW,
+                                           TileStatus st, bool famA, long long lt, unsigned long long len, int* err,
+                                           unsigned long long* sm, unsigned long long* s_base) {
+    static_assert((unsigned long long)kIdxThreads * kIdxItems == kIdxPerTile, "index tile size");
+    const unsigned long long nw = (h.nb + 31) / 32;
+    const unsigned long long first = (unsigned long long)lt * kIdxPerTile + threadIdx.x * kIdxItems;
+    unsigned long long vals[kIdxItems];
+    unsigned long long mine = 0;
+#pragma unroll
+    for (int i = 0; i < kIdxItems; i++) {
+        unsigned long long k = first + i;
+        unsigned long long v = 0;
+        if (famA) {
+            if (k < h.nnc) v = (unsigned long long)s[h.o_off + 2 * k] | ((unsigned long long)s[h.o_off + 2 * k + 1] << 8);
+        } else if (k < nw) {
+            uint32_t w = 0;
+            for (int j = 0; j < 4; j++) {
+                unsigned long long bi = 4 * k + j;
+                w = (w << 8) | (bi < h.sb ? s[h.s_off + bi] : 0u);
+            }
+            v = __popc(w);
+        }
+        vals[i] = v;
+        mine += v;
+    }
+    unsigned long long tot;
+    unsigned long long ex = cta_exclusive_sum(mine, &tot, sm);
+    if (threadIdx.x < 32) {
+        unsigned long long ba, bb;
+        lookback(st, lt, tot, 0, &ba, &bb, err);
+        if (threadIdx.x == 0) *s_base = ba;
+    }
+    __syncthreads();
+    unsigned long long run = *s_base + ex;
+#pragma unroll
+    for (int i = 0; i < kIdxItems; i++) {
+        unsigned long long k = first + i;
+        if (famA) {
+            if (k < h.nnc) P[k] = run;
+            if (k == h.nnc - 1) {
+                P[h.nnc] = run + vals[i];
+                if (h.q_off + run + vals[i] > len) atomicExch(err, kErrStream);
+            }
+        } else if (k < nw) {
+            RW[k] = (uint32_t)run;
+        }
+        run += vals[i];
+    }
+    __syncthreads();
+}
+
+// The scans of one stream in one persistent launch (family A first).
 __global__ void __launch_bounds__(kIdxThreads) k_blocked_index(const uint8_t* s, const BlockedHdr* hp,
                                                                unsigned long long* P, uint32_t* RW,
                                                                TileStatus stA, TileStatus stB,
@@ -833,59 +902,53 @@ __global__ void __launch_bounds__(kIdxThreads) k_blocked_index(const uint8_t* s,
     __shared__ unsigned long long s_base;
     const BlockedHdr h = *hp;
     if (!h.ok) return;
-    constexpr unsigned long long per = (unsigned long long)kIdxThreads * kIdxItems;
     const unsigned long long nw = (h.nb + 31) / 32;
-    const long long TA = famA ? (long long)((h.nnc + per - 1) / per) : 0;   // no size index in fastMode 2
-    const long long TBt = (long long)((nw + per - 1) / per);
+    const long long TA = famA ? (long long)((h.nnc + kIdxPerTile - 1) / kIdxPerTile) : 0;   // no size index in fastMode 2
+    const long long TBt = (long long)((nw + kIdxPerTile - 1) / kIdxPerTile);
     for (;;) {
         if (threadIdx.x == 0) s_tile = (long long)atomicAdd(ctr, 1ull);
         __syncthreads();
         long long t = s_tile;
         if (t >= TA + TBt) break;
-        const bool famA = t < TA;
-        const long long lt = famA ? t : t - TA;
-        const unsigned long long first = (unsigned long long)lt * per + threadIdx.x * kIdxItems;
-        unsigned long long vals[kIdxItems];
-        unsigned long long mine = 0;
-#pragma unroll
-        for (int i = 0; i < kIdxItems; i++) {
-            unsigned long long k = first + i;
-            unsigned long long v = 0;
-            if (famA) {
-                if (k < h.nnc) v = (unsigned long long)s[h.o_off + 2 * k] | ((unsigned long long)s[h.o_off + 2 * k + 1] << 8);
-            } else if (k < nw) {
-                uint32_t w = 0;
-                for (int j = 0; j < 4; j++) {
-                    unsigned long long bi = 4 * k + j;
-                    w = (w << 8) | (bi < h.sb ? s[h.s_off + bi] : 0u);
-                }
-                v = __popc(w);
+        const bool fa = t < TA;
+        index_tile(s, h, P, RW, fa ? stA : stB, fa, fa ? t : t - TA, len, err, sm, &s_base);
+    }
+}
+
+// The scans of every stream of a batch: tiles in field order (each field's
+// offset tiles, then its rank tiles) from one counter; a field whose header
+// failed, and offset tiles past a field's real nnc, do nothing.
+__global__ void __launch_bounds__(kIdxThreads) k_blocked_index_fields(const DecField* F, int nf,
+                                                                      unsigned long long total,
+                                                                      unsigned long long* ctr) {
+    __shared__ unsigned long long sm[8];
+    __shared__ long long s_tile;
+    __shared__ int s_f;
+    __shared__ unsigned long long s_base;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long g = (long long)atomicAdd(ctr, 1ull);
+            int lo = 0, hi = nf - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if ((long long)F[mid].idx_tile0 <= g) lo = mid;
+                else hi = mid - 1;
             }
-            vals[i] = v;
-            mine += v;
-        }
-        unsigned long long tot;
-        unsigned long long ex = cta_exclusive_sum(mine, &tot, sm);
-        if (threadIdx.x < 32) {
-            unsigned long long ba, bb;
-            lookback(famA ? stA : stB, lt, tot, 0, &ba, &bb, err);
-            if (threadIdx.x == 0) s_base = ba;
+            s_tile = g;
+            s_f = lo;
         }
         __syncthreads();
-        unsigned long long run = s_base + ex;
-#pragma unroll
-        for (int i = 0; i < kIdxItems; i++) {
-            unsigned long long k = first + i;
-            if (famA) {
-                if (k < h.nnc) P[k] = run;
-                if (k == h.nnc - 1) {
-                    P[h.nnc] = run + vals[i];
-                    if (h.q_off + run + vals[i] > len) atomicExch(err, kErrStream);
-                }
-            } else if (k < nw) {
-                RW[k] = (uint32_t)run;
-            }
-            run += vals[i];
+        const long long g = s_tile;
+        if (g >= (long long)total) break;
+        const DecField& D = F[s_f];
+        const BlockedHdr h = *D.hdr;
+        const long long local = g - (long long)D.idx_tile0;
+        const bool fa = local < (long long)D.idxA_tiles;
+        const long long lt = fa ? local : local - (long long)D.idxA_tiles;
+        const long long TA = (long long)((h.nnc + kIdxPerTile - 1) / kIdxPerTile);
+        if (h.ok && (!fa || lt < TA)) {
+            const TileStatus st = fa ? TileStatus{D.stA[0], D.stA[1], D.stA[2]} : TileStatus{D.stB[0], D.stB[1], D.stB[2]};
+            index_tile(D.s, h, D.P, D.RW, st, fa, lt, D.len, D.err, sm, &s_base);
         }
         __syncthreads();
     }
@@ -1078,12 +1141,15 @@ struct DecArgs {
     const uint32_t* RW;            // non-constant rank at each 32-block state word
     void* out;
     int native_medians;
-    int* err;
+    int* err;                      // one stream: its error word; a batch: the launch's (bounded waits)
+    const DecField* fields;        // a batch: the field table (ascending dec_tile0), else unused
+    int nf, bs;
+    unsigned long long total_tiles;
 };
 
 enum : uint8_t { kBlkConst = 0, kBlkCoded = 1, kBlkNone = 2 };
 
-template <typename T, int G>
+template <typename T, int G, bool MULTI>
 __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
     using TL = DecTileV<T, G>;
     constexpr int TB = TL::kBlocks;
@@ -1093,13 +1159,17 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
     __shared__ uint32_t s_info[NS][TB];    // coded: payload position in the stage; constant: median bits
     __shared__ uint8_t s_kind[NS][TB];
     __shared__ uint8_t s_ok[NS];
+    __shared__ int s_fld[NS];              // a batch: the tile's field
     __shared__ uint16_t s_rank[TB];        // producer scratch: rank within the tile
     __shared__ uint32_t lut_ld[256], lut_cm[256];
-    const BlockedHdr h = *a.hdr;
-    if (!h.ok) return;
-    if (h.bs > (unsigned long long)TL::kBsMax) {
-        if (threadIdx.x == 0 && blockIdx.x == 0) atomicExch(a.err, kErrStream);
-        return;
+    BlockedHdr h = {};
+    if constexpr (!MULTI) {
+        h = *a.hdr;
+        if (!h.ok) return;
+        if (h.bs > (unsigned long long)TL::kBsMax) {
+            if (threadIdx.x == 0 && blockIdx.x == 0) atomicExch(a.err, kErrStream);
+            return;
+        }
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -1111,9 +1181,18 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
     }
     lead_tables_init(lut_ld, lut_cm);
     __syncthreads();
-    const unsigned long long nb = h.nb;
-    const long long ntiles = (long long)((nb + TB - 1) / TB);
-    const int bs = (int)h.bs;
+    const long long ntiles = MULTI ? (long long)a.total_tiles : (long long)((h.nb + TB - 1) / TB);
+    const int bs = MULTI ? a.bs : (int)h.bs;
+    // field of a launch-wide tile (batch)
+    auto field_of = [&](long long g) {
+        int lo = 0, hi = a.nf - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((long long)a.fields[mid].dec_tile0 <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    };
 
     if (warp == kDecWarps) {
         // ---------------------------------------------------------- producer
@@ -1125,8 +1204,24 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
                 break;
             }
             uint8_t* stage = dsm + slot * TL::kStage;
-            const unsigned long long b0 = (unsigned long long)t * TB;
-            const unsigned long long rest = nb - b0;
+            // the tile's stream: the launch's, or its field's
+            const uint8_t* S = a.s;
+            unsigned long long L = a.len;
+            const unsigned long long* P = a.P;
+            const uint32_t* RW = a.RW;
+            int* ferr = a.err;
+            BlockedHdr hh = h;
+            long long lt = t;
+            if constexpr (MULTI) {
+                const int f = field_of(t);
+                const DecField* D = a.fields + f;
+                S = D->s; L = D->len; P = D->P; RW = D->RW; ferr = D->err;
+                hh = *D->hdr;
+                lt = t - (long long)D->dec_tile0;
+                if (lane == 0) s_fld[slot] = f;
+            }
+            const unsigned long long b0 = (unsigned long long)lt * TB;
+            const unsigned long long rest = hh.ok ? hh.nb - b0 : 0;   // a batch's failed header: no blocks
             const int nblk = rest < (unsigned long long)TB ? (int)rest : TB;
             // rank of the tile's first block
             const unsigned long long w = b0 >> 5;
@@ -1135,16 +1230,16 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const unsigned long long bi = 4 * w + j;
-                word = (word << 8) | (bi < h.sb ? (uint32_t)a.s[h.s_off + bi] : 0u);
+                word = (word << 8) | (bi < hh.sb ? (uint32_t)S[hh.s_off + bi] : 0u);
             }
-            const unsigned long long rank0 = a.RW[w] + (bit0 ? __popc(word >> (32 - bit0)) : 0);
+            const unsigned long long rank0 = hh.ok ? RW[w] + (bit0 ? __popc(word >> (32 - bit0)) : 0) : 0;
             // state of every block; medians of the constant ones
             uint32_t ok = 1, running = 0;
             for (int j = 0; j < TB; j += 32) {
                 const int lb = j + lane;
                 const unsigned long long b = b0 + lb;
                 const bool in = lb < nblk;
-                const uint32_t coded = in ? (a.s[h.s_off + (b >> 3)] >> (7 - (b & 7))) & 1u : 0u;
+                const uint32_t coded = in ? (S[hh.s_off + (b >> 3)] >> (7 - (b & 7))) & 1u : 0u;
                 const unsigned m = __ballot_sync(0xffffffffu, coded);
                 const uint32_t r = running + __popc(m & ((1u << lane) - 1));
                 running += __popc(m);
@@ -1155,10 +1250,10 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
                         s_kind[slot][lb] = kBlkCoded;
                         s_rank[lb] = (uint16_t)r;
                     } else {
-                        const unsigned long long mo = h.m_off + 4 * (b - (rank0 + r));
+                        const unsigned long long mo = hh.m_off + 4 * (b - (rank0 + r));
                         uint32_t mbits = 0;
-                        if (b >= rank0 + r && mo + 4 <= h.q_off) {
-                            const uint8_t* mp = a.s + mo;
+                        if (b >= rank0 + r && mo + 4 <= hh.q_off) {
+                            const uint8_t* mp = S + mo;
                             mbits = a.native_medians
                                         ? ((uint32_t)mp[0] | ((uint32_t)mp[1] << 8) | ((uint32_t)mp[2] << 16) |
                                            ((uint32_t)mp[3] << 24))
@@ -1174,23 +1269,23 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
             }
             const uint32_t nnc_t = running;
             unsigned long long pa = 0, pb = 0;
-            if (rank0 + nnc_t > h.nnc) ok = 0;
+            if (rank0 + nnc_t > hh.nnc) ok = 0;
             if (__all_sync(0xffffffffu, ok) && nnc_t) {
-                pa = a.P[rank0];
-                pb = a.P[rank0 + nnc_t];
-                if (pb < pa || pb - pa > (unsigned long long)TB * TL::kMaxPay || h.q_off + pb > a.len) ok = 0;
+                pa = P[rank0];
+                pb = P[rank0 + nnc_t];
+                if (pb < pa || pb - pa > (unsigned long long)TB * TL::kMaxPay || hh.q_off + pb > L) ok = 0;
             }
             __syncwarp();
-            const uint8_t* src = a.s + h.q_off + pa;
+            const uint8_t* src = S + hh.q_off + pa;
             const uint32_t ph = (uint32_t)((uintptr_t)src & 15);
             if (__all_sync(0xffffffffu, ok) && nnc_t) {
                 for (int j = 0; j < TB; j += 32) {
                     const int lb = j + lane;
                     if (lb < nblk && s_kind[slot][lb] == kBlkCoded) {
                         const unsigned long long k = rank0 + s_rank[lb];
-                        const unsigned long long p0 = a.P[k], p1 = a.P[k + 1];
-                        const unsigned long long rem = h.n - (b0 + lb) * h.bs;
-                        const int blen = rem < h.bs ? (int)rem : bs;
+                        const unsigned long long p0 = P[k], p1 = P[k + 1];
+                        const unsigned long long rem = hh.n - (b0 + lb) * hh.bs;
+                        const int blen = rem < hh.bs ? (int)rem : bs;
                         const unsigned long long minsz = 5 + (unsigned long long)((blen + 3) / 4);
                         if (p0 < pa || p1 > pb || p1 < p0 + minsz || p1 - p0 > (unsigned long long)TL::kMaxPay) ok = 0;
                         s_info[slot][lb] = ph + (uint32_t)(p0 - pa);
@@ -1215,7 +1310,7 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
             __syncwarp();
             if (lane == 0) {
                 s_ok[slot] = (uint8_t)ok;
-                if (!ok) atomicExch(a.err, kErrStream);
+                if (!ok) atomicExch(ferr, kErrStream);
                 fence_proxy_async();
                 mbar_arrive_expect_tx(&full[slot], tx);
                 if (tx) tma_load_1d(stage + ph + (a0 - sa), (const void*)a0, tx, &full[slot]);
@@ -1228,7 +1323,8 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
 
     // -------------------------------------------------------------- consumers
     T* out = (T*)a.out;
-    const bool vec = ((bs * (int)sizeof(T)) & 15) == 0 && ((uintptr_t)out & 15) == 0;
+    bool vec = ((bs * (int)sizeof(T)) & 15) == 0 && ((uintptr_t)out & 15) == 0;
+    unsigned long long n = h.n;
     const int seg = lane / G;
     const int lb = warp * TL::kBpw + seg;
     long long i = 0;
@@ -1238,14 +1334,22 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
             if (lane == 0) atomicExch(a.err, kErrLookback);
             break;
         }
-        const unsigned long long b = (unsigned long long)t * TB + lb;
+        long long lt = t;
+        if constexpr (MULTI) {
+            const DecField* D = a.fields + s_fld[slot];
+            out = (T*)D->out;
+            n = D->n;
+            lt = t - (long long)D->dec_tile0;
+            vec = ((bs * (int)sizeof(T)) & 15) == 0 && ((uintptr_t)out & 15) == 0;
+        }
+        const unsigned long long b = (unsigned long long)lt * TB + lb;
         const int kind = s_kind[slot][lb];
         const uint32_t info = s_info[slot][lb];
         int blen = 0;
         T* ob = out;
         if (kind != kBlkNone) {
-            const unsigned long long off = b * h.bs, rem = h.n - off;
-            blen = rem < h.bs ? (int)rem : bs;
+            const unsigned long long off = b * (unsigned long long)bs, rem = n - off;
+            blen = rem < (unsigned long long)bs ? (int)rem : bs;
             ob = out + off;
         }
         if (kind == kBlkConst) {
@@ -1267,27 +1371,119 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
     }
 }
 
-template <typename T, int G>
-static cudaError_t run_decode(const uint8_t* s, size_t len, size_t nb, const Workspace& ws, void* out, int native,
-                              cudaStream_t st) {
-    using TL = DecTileV<T, G>;
+template <typename T, int G, bool MULTI>
+static cudaError_t dec_attr() {
     static bool attr_set[64] = {false};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_blocked_decode<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             TL::kDynSmem);
+        cudaError_t e = cudaFuncSetAttribute(k_blocked_decode<T, G, MULTI>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, DecTileV<T, G>::kDynSmem);
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
+    return cudaSuccess;
+}
+
+template <typename T, int G>
+static cudaError_t run_decode(const uint8_t* s, size_t len, size_t nb, const Workspace& ws, void* out, int native,
+                              cudaStream_t st) {
+    using TL = DecTileV<T, G>;
+    cudaError_t e = dec_attr<T, G, false>();
+    if (e != cudaSuccess) return e;
     const size_t tiles = (nb + TL::kBlocks - 1) / TL::kBlocks;
     const size_t cap = (size_t)sm_count() * 3;
     const int grid = (int)(tiles < cap ? (tiles ? tiles : 1) : cap);
-    DecArgs a;
+    DecArgs a = {};
     a.s = s; a.len = len; a.hdr = ws.bhdr; a.P = ws.p_off; a.RW = ws.rank_w; a.out = out;
     a.native_medians = native; a.err = ws.err;
     TraceScope tr("blocked_decode", st);
-    k_blocked_decode<T, G><<<grid, kDecThreadsP, TL::kDynSmem, st>>>(a);
+    k_blocked_decode<T, G, false><<<grid, kDecThreadsP, TL::kDynSmem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T, int G>
+static cudaError_t run_decode_fields(const DecField* F, int nf, int bs, unsigned long long total, int native,
+                                     int* lerr, cudaStream_t st) {
+    using TL = DecTileV<T, G>;
+    cudaError_t e = dec_attr<T, G, true>();
+    if (e != cudaSuccess) return e;
+    const size_t cap = (size_t)sm_count() * 3;
+    const int grid = (int)(total < cap ? (total ? total : 1) : cap);
+    DecArgs a = {};
+    a.native_medians = native; a.err = lerr;
+    a.fields = F; a.nf = nf; a.bs = bs; a.total_tiles = total;
+    TraceScope tr("blocked_decode_fields", st);
+    k_blocked_decode<T, G, true><<<grid, kDecThreadsP, TL::kDynSmem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Lanes per block as in the encoder: 16 (float) / 8 (double) values per lane.
+static int dec_lanes(int dtype, int bs) {
+    const int per = dtype == 0 ? 16 : 8;
+    const int need = (bs + per - 1) / per;
+    return need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
+}
+
+int blocked_dec_tile_blocks(int dtype, int bs) { return kDecWarps * (32 / dec_lanes(dtype, bs)); }
+
+// Per-field outcome of a batched decode; *err gets the first failing status.
+__global__ void k_blocked_decode_finish(const DecField* F, int nf, int esize, StreamResult* res, const int* lerr,
+                                        int* err) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const DecField& D = F[f];
+    int st = *D.err;
+    if (!st) st = *lerr;
+    StreamResult r;
+    r.offset = 0;
+    r.size = D.n * (unsigned long long)esize;
+    r.nb_const = D.hdr->ok ? D.hdr->nc : 0;
+    r.eb = 0.f;
+    r.status = st;
+    res[f] = r;
+    if (st) atomicCAS(err, 0, st);
+}
+
+cudaError_t launch_blocked_decode_fields(int layout, int dtype, int bs, int nf, const DecField* d_fields,
+                                         unsigned long long idx_total, unsigned long long dec_total,
+                                         unsigned long long* counters, StreamResult* res, int* err,
+                                         cudaStream_t s) {
+    if (layout != kRandomAccess && layout != kRandomAccessNative) return cudaErrorInvalidValue;
+    if (bs < 1 || bs > 256 || nf < 1) return cudaErrorInvalidValue;
+    int* lerr = (int*)(counters + 3);
+    {
+        TraceScope tr("blocked_parse_fields", s);
+        k_blocked_parse_fields<<<(nf + 127) / 128, 128, 0, s>>>(d_fields, nf, (unsigned long long)bs);
+    }
+    {
+        const unsigned long long cap = (unsigned long long)sm_count() * 4;
+        const int ig = (int)(idx_total < cap ? (idx_total ? idx_total : 1) : cap);
+        TraceScope tr("blocked_index_fields", s);
+        k_blocked_index_fields<<<ig, kIdxThreads, 0, s>>>(d_fields, nf, idx_total, &counters[0]);
+    }
+    const int native = layout == kRandomAccessNative;
+    cudaError_t e;
+    if (dtype == 0) {
+        switch (dec_lanes(dtype, bs)) {
+            case 1: e = run_decode_fields<float, 1>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 2: e = run_decode_fields<float, 2>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 4: e = run_decode_fields<float, 4>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 8: e = run_decode_fields<float, 8>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            default: e = run_decode_fields<float, 16>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+        }
+    } else {
+        switch (dec_lanes(dtype, bs)) {
+            case 1: e = run_decode_fields<double, 1>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 2: e = run_decode_fields<double, 2>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 4: e = run_decode_fields<double, 4>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 8: e = run_decode_fields<double, 8>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 16: e = run_decode_fields<double, 16>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            default: e = run_decode_fields<double, 32>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+        }
+    }
+    if (e != cudaSuccess) return e;
+    k_blocked_decode_finish<<<(nf + 127) / 128, 128, 0, s>>>(d_fields, nf, dtype == 0 ? 4 : 8, res, lerr, err);
     return cudaGetLastError();
 }
 
@@ -1319,10 +1515,7 @@ cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream
     // is validated again by every kernel and a mismatch is reported, not used.
     const int native = layout == kRandomAccessNative;
     const size_t nb = (n + bs - 1) / bs;
-    // lanes per block as in the encoder: 16 (float) / 8 (double) values per lane
-    const int per = dtype == 0 ? 16 : 8;
-    const int need = (bs + per - 1) / per;
-    const int G = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
+    const int G = dec_lanes(dtype, bs);
     if (dtype == 0) {
         switch (G) {
             case 1: e = run_decode<float, 1>(d_stream, len, nb, ws, d_out, native, s); break;

@@ -78,6 +78,24 @@ struct BlkField {
     StreamResult* res;
 };
 
+// One stream of a batched blocked decode (fastMode 3/4).  Tile counts are
+// known from n alone: the payload-offset scan is given ceil(nb / 2048) tiles
+// (nnc <= nb) and skips those past the stream's real nnc.
+struct DecField {
+    const uint8_t* s;                            // stream (device)
+    unsigned long long len, n, nb;               // stream bytes, values, blocks
+    void* out;                                   // values (device)
+    BlockedHdr* hdr;                             // parsed header
+    unsigned long long* P;                       // [nb + 1] payload offsets by non-constant rank
+    uint32_t* RW;                                // [nb / 32 + 2] rank at each 32-block state word
+    unsigned long long* stA[3];                  // offset-scan look-back: word, agg2, inc2 [idxA_tiles], zeroed
+    unsigned long long* stB[3];                  // rank-scan look-back [idxB_tiles], zeroed
+    unsigned long long idx_tile0, idxA_tiles, idxB_tiles;   // launch-wide first index tile, tiles per scan
+    unsigned long long dec_tile0, dec_tiles;     // launch-wide first decode tile, decode tiles
+    int* err;                                    // this stream's error word, zeroed
+    int pad;
+};
+
 // ------------------------------------------------------------------ workspace
 
 // Device scratch needed by one compress or decompress call; carved by
@@ -181,6 +199,17 @@ int blocked_tile_blocks(int dtype, int bs);
 cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, const BlkField& one,
                                          const BlkField* d_fields, unsigned long long enc_total,
                                          unsigned long long asm_total, unsigned long long* counters, int* err,
+                                         cudaStream_t s);
+// Blocked decode of nf streams (layouts 3, 4) in one launch per kernel: the
+// headers are parsed into the fields' hdr, counters[0] and every field's
+// look-back words and error word zeroed by the caller; res[f] receives field
+// f's outcome and *err the first failing status.  idx_total / dec_total: the
+// launch-wide index and decode tiles (sums over the table).
+int blocked_dec_tile_blocks(int dtype, int bs);
+constexpr unsigned long long kIdxPerTile = 2048;   // items per tile of the index scans
+cudaError_t launch_blocked_decode_fields(int layout, int dtype, int bs, int nf, const DecField* d_fields,
+                                         unsigned long long idx_total, unsigned long long dec_total,
+                                         unsigned long long* counters, StreamResult* res, int* err,
                                          cudaStream_t s);
 // Blocked decode (layouts 3, 4).
 cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream, size_t len, size_t n, int bs,

@@ -33,6 +33,7 @@ def env():
     L.SZxG_batch_status.restype = C.c_int
     L.SZxG_batch_status.argtypes = [C.c_void_p, C.c_void_p]
     L.SZxG_batch_destroy.restype = None
+    L.SZxG_workspace_status.restype = C.c_int
     L.SZxG_batch_destroy.argtypes = [C.c_void_p]
     return torch, L, StreamInfo
 
@@ -142,3 +143,104 @@ def test_batch_replays_from_a_cuda_graph(env):
     want = _batch(env, 3, xs, 128, ebs)
     got = _batch(env, 3, xs, 128, ebs, graph=True)
     assert got == want
+
+
+def _single_decompress(env, mode, stream, n, bs, dt):
+    torch, L, StreamInfo = env
+    code = 0 if dt == torch.float32 else 1
+    wsb = L.SZxG_workspace_size(mode, code, n, bs)
+    ws = torch.zeros(wsb, dtype=torch.uint8, device="cuda")
+    out = torch.empty(n, dtype=dt, device="cuda")
+    rc = L.SZxG_decompress(mode, code, C.c_void_p(stream.data_ptr()), stream.numel(), n, bs,
+                           C.c_void_p(out.data_ptr()), C.c_void_p(ws.data_ptr()), wsb,
+                           C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0
+    assert L.SZxG_workspace_status(C.c_void_p(ws.data_ptr()), C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+    return out
+
+
+def _batch_decompress(env, mode, streams, ns, bs, dt, graph=False):
+    """Decode device streams as one batch; returns (values per field, status per field, batch status)."""
+    torch, L, StreamInfo = env
+    code = 0 if dt == torch.float32 else 1
+    outs, fields = [], (Field * len(streams))()
+    for k, (s, n) in enumerate(zip(streams, ns)):
+        o = torch.full((n,), 7.0, dtype=dt, device="cuda")
+        outs.append(o)
+        fields[k] = Field(s.data_ptr(), n, s.numel(), 0.0, 0, o.data_ptr(), o.numel() * o.element_size())
+    b = L.SZxG_batch_create(1, mode, code, bs, len(streams), C.cast(fields, C.c_void_p))
+    assert b, L.SZxG_error_string(L.SZxG_get_last_error())
+    info = torch.zeros(len(streams) * C.sizeof(StreamInfo), dtype=torch.uint8, device="cuda")
+    try:
+        if graph:
+            g = torch.cuda.CUDAGraph()
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                assert L.SZxG_batch_run(b, C.c_void_p(info.data_ptr()), C.c_void_p(s.cuda_stream)) == 0
+            torch.cuda.current_stream().wait_stream(s)
+            torch.cuda.synchronize()
+            with torch.cuda.graph(g):
+                assert L.SZxG_batch_run(b, C.c_void_p(info.data_ptr()),
+                                        C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+            torch.cuda.synchronize()
+            for o in outs:
+                o.fill_(7.0)
+            info.zero_()
+            g.replay()
+            g.replay()
+        else:
+            assert L.SZxG_batch_run(b, C.c_void_p(info.data_ptr()),
+                                    C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+        st = L.SZxG_batch_status(b, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        raw = info.cpu().numpy().tobytes()
+        infos = [StreamInfo.from_buffer_copy(raw[k * C.sizeof(StreamInfo):(k + 1) * C.sizeof(StreamInfo)])
+                 for k in range(len(streams))]
+        return outs, infos, st
+    finally:
+        L.SZxG_batch_destroy(b)
+
+
+def _same(a, b):
+    """Bitwise equality of two float tensors."""
+    import torch
+    it = torch.int32 if a.element_size() == 4 else torch.int64
+    return a.shape == b.shape and bool((a.view(it) == b.view(it)).all())
+
+
+@pytest.mark.parametrize("mode,dtname,bs", [(3, "float32", 128), (4, "float64", 64), (3, "float64", 256),
+                                            (4, "float32", 16), (3, "float32", 1)])
+def test_batch_decompress_equals_single_stream_decompress(env, mode, dtname, bs):
+    torch = env[0]
+    dt = getattr(torch, dtname)
+    rng = np.random.default_rng(9)
+    hi = 1 << 17 if bs == 1 else 1 << 21
+    sizes = [1, 2, 127, 128, 129, 4097, 65536] + [int(v) for v in np.exp(rng.uniform(np.log(1 << 14),
+                                                                                       np.log(hi), 30))]
+    xs, ebs = _fields(torch, dt, sizes, 13)
+    streams = [torch.tensor(np.frombuffer(s, np.uint8).copy(), device="cuda")
+               for s in _batch(env, mode, xs, bs, ebs)]
+    outs, infos, st = _batch_decompress(env, mode, streams, sizes, bs, dt)
+    assert st == 0
+    for k, (s, n) in enumerate(zip(streams, sizes)):
+        assert infos[k].status == 0 and infos[k].size == n * xs[k].element_size()
+        want = _single_decompress(env, mode, s, n, bs, dt)
+        assert _same(outs[k], want), (k, n)
+
+
+def test_batch_decompress_isolates_bad_streams_and_replays(env):
+    """A truncated stream and one of another block size fail alone; the rest
+    decode exactly, also when the batch is replayed from a CUDA graph."""
+    torch = env[0]
+    sizes = [70001, 1 << 18, 5000, 1 << 20, 333]
+    xs, ebs = _fields(torch, torch.float32, sizes, 17)
+    streams = [torch.tensor(np.frombuffer(s, np.uint8).copy(), device="cuda")
+               for s in _batch(env, 3, xs, 128, ebs)]
+    other_bs = torch.tensor(np.frombuffer(_single(env, 3, xs[2], 64, ebs[2]), np.uint8).copy(), device="cuda")
+    bad = [streams[0], streams[1][: streams[1].numel() // 2].clone(), other_bs, streams[3], streams[4]]
+    for graph in (False, True):
+        outs, infos, st = _batch_decompress(env, 3, bad, sizes, 128, torch.float32, graph=graph)
+        assert st == 3
+        assert [i.status for i in infos] == [0, 3, 3, 0, 0]
+        for k in (0, 3, 4):
+            assert _same(outs[k], _single_decompress(env, 3, streams[k], sizes[k], 128, torch.float32)), k
