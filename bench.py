@@ -46,6 +46,11 @@ WORKLOADS = {
                      "(profiling size: 216 MiB, above L2)"),
     "c2m1": dict(shape=(512, 512, 512), mode=1, bs=128, rel=1e-3,
                  desc="512^3 float32 k^-5/3 Gaussian random field + 5% zero slabs, REL 1e-3, fastMode 1"),
+    "c5": dict(mode=2, bs=128,
+               desc="learned fixed rate: 500 float32 fields, sizes log-uniform 2^20..2^26, seeded mix of spectral / "
+                    "piecewise-constant (+1e-3 noise) / white noise, targets 8, 16, 32 within 5%, fastMode-2 "
+                    "streams, blockSize 128; network trained on the GPU from 20 real compress passes of 1000 "
+                    "other fields of the same distribution"),
     "c4": dict(mode=3, bs=128,
                desc="batched: float32 fields, sizes log-uniform 2^14..2^26, seeded mix of spectral / "
                     "piecewise-constant / white noise, per-field ABS bound log-uniform 1e-5..1e-2 x range, "
@@ -373,6 +378,75 @@ def make_batch_fields(nf, seed, device):
     return xs, ebs
 
 
+def run_fixed_rate(args, wl):
+    """C5: fixed-rate selection for 500 fields x 3 targets -- the learned path
+    (sampled model + network, judged by real compress passes) against plain
+    bisection over real compress passes, on the same GPU and plan."""
+    import numpy as np
+    import torch
+
+    from szx_gb300 import learned as LR
+    t0 = time.perf_counter()
+    tf, _ = LR.synthetic_fields(1000, 20, 26, seed=101)
+    tb = LR.Batch(tf)
+    X, y, _ = LR.training_set(tb, passes=20, seed=102)
+    tb.close()
+    del tf, tb
+    torch.cuda.empty_cache()
+    t1 = time.perf_counter()
+    model, loss = LR.train(X, y, seed=103, epochs=100, batch=512)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    rows, var = int(X.shape[0]), float(y.var())
+    del X, y
+    zero = LR.Mlp(0, params=np.concatenate([np.zeros(32), np.ones(32),
+                                            np.zeros(model.count - 64)]).astype(np.float32))
+    fields, _ = LR.synthetic_fields(500, 20, 26, seed=202)
+    b = LR.Batch(fields)
+    nbytes = float(b.n.sum() * 4)
+    b.fixed_rate(8.0, model, 0.05, 20)   # warm-up
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    time.sleep(0.3)
+    per = {}
+    tot = {"bisection": 0.0, "learned": 0.0, "zero_network": 0.0}
+    jobs = 0
+    for target in (8.0, 16.0, 32.0):
+        per[target] = {}
+        for name, m in (("bisection", None), ("zero_network", zero), ("learned", model)):
+            torch.cuda.synchronize()
+            ts = time.perf_counter()
+            eb, cr, ps = b.fixed_rate(target, m, 0.05, 20)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - ts
+            tot[name] += dt
+            ok = np.abs(cr / target - 1) <= 0.05
+            per[target][name] = {"fields_per_s": round(b.nf / dt, 2), "ok": round(float(ok.mean()), 4),
+                                 "passes_mean": round(float(ps.mean()), 3), "first_pass_hits": round(float((ps == 1).mean()), 4),
+                                 "median_abs_miss": round(float(np.median(np.abs(cr / target - 1))), 4)}
+        jobs += b.nf
+    clk = clocks.stop()
+    b.close()
+    fps = {k: jobs / v for k, v in tot.items()}
+    line = {
+        "metric": "fixed-rate fields/s at +/-5% ratio", "value": round(fps["learned"], 2), "unit": "fields/s",
+        "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": round(1000 * tot["learned"], 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded on-device fields)",
+        "config": {"workload": wl["desc"], "fields": 500, "targets": [8, 16, 32], "tolerance": 0.05,
+                   "max_passes": 20, "field_bytes": int(nbytes)},
+        "bisection_fields_per_s": round(fps["bisection"], 2),
+        "speedup_vs_bisection": round(fps["learned"] / fps["bisection"], 2),
+        "zero_network_fields_per_s": round(fps["zero_network"], 2),
+        "learned_gbs": round(nbytes * 3 / tot["learned"] / 1e9, 1),
+        "per_target": {str(int(k)): v for k, v in per.items()},
+        "training": {"rows": rows, "label_var": round(var, 5), "final_mse": round(loss, 5),
+                     "corpus_s": round(t1 - t0, 1), "train_s": round(t2 - t1, 2)},
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
 def run_batched(args, wl):
     """C4: one batch (one persistent launch per kernel, replayed from a CUDA
     graph) against the same fields compressed by per-field calls."""
@@ -560,6 +634,9 @@ def main():
         return
     if args.workload == "c4":
         run_batched(args, wl)
+        return
+    if args.workload == "c5":
+        run_fixed_rate(args, wl)
         return
     if world > 1:
         import torch

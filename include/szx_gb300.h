@@ -213,6 +213,50 @@ int SZxG_batch_run(SZxG_Batch* batch, SZxG_StreamInfo* d_info, void* stream);
 int SZxG_batch_status(SZxG_Batch* batch, void* stream);
 void SZxG_batch_destroy(SZxG_Batch* batch);
 
+/* Change the bounds of a compress plan's fields and which fields a run codes:
+ * fieldIndex[k] (k < nActive) in that order, all fields when fieldIndex is
+ * NULL (nActive == nFields); absErrBound[k] is field fieldIndex[k]'s new bound
+ * (NULL keeps the bounds).  Ordered on `stream`.  A graph captured before a
+ * call that changes the set of fields must be captured again; one that only
+ * changes bounds stays valid (the bounds are read from device memory). */
+int SZxG_batch_set_bounds(SZxG_Batch* batch, int nActive, const int* fieldIndex, const float* absErrBound,
+                          void* stream);
+
+/* ---------------------------------------------------------------- fixed rate, learned
+ * A small network predicts the bound that gives a target compression ratio
+ * from 32 features of every 10th block; real compress passes of the whole
+ * batch judge it (float fields, blockSize 128).  Features of a field, row
+ * layout of X (SZXG_FXR_FEATURES floats): see szx_gb300/csrc/learned.cu. */
+#define SZXG_FXR_FEATURES 32
+typedef struct SZxG_Mlp SZxG_Mlp;
+size_t SZxG_mlp_param_count(void);
+SZxG_Mlp* SZxG_mlp_create(unsigned long long seed);          /* Xavier-uniform initial weights */
+void SZxG_mlp_destroy(SZxG_Mlp* mlp);
+int SZxG_mlp_get_params(const SZxG_Mlp* mlp, float* params, size_t count);
+int SZxG_mlp_set_params(SZxG_Mlp* mlp, const float* params, size_t count);
+/* d_out[i] = the network's output for feature row i: the predicted miss
+ * log2(real ratio / target) at the sampled curve's crossing (feature 1). */
+int SZxG_mlp_forward(const SZxG_Mlp* mlp, const float* d_X, size_t n, float* d_out, void* stream);
+/* Gradient of the mean squared error over n rows (trainable parameters, in
+ * order W1 b1 W2 b2 W3 b3 W4 b4) and the error itself (synchronous). */
+int SZxG_mlp_gradient(SZxG_Mlp* mlp, const float* d_X, const float* d_y, size_t n, float* d_grad, float* loss,
+                      void* stream);
+/* Adam on minibatches; input statistics and output bias set from the data. */
+int SZxG_mlp_train(SZxG_Mlp* mlp, const float* d_X, const float* d_y, size_t n, int epochs, int batch, float lr,
+                   unsigned long long seed, float* loss, void* stream);
+/* Feature rows of a compress plan's fields: row r describes field
+ * fieldOfRow[r] for targetRatio[r]; h_range[nFields] receives each field's
+ * sampled range (synchronous). */
+int SZxG_batch_features(SZxG_Batch* batch, int nRows, const int* fieldOfRow, const float* targetRatio, float* d_X,
+                        float* h_range, void* stream);
+/* Choose every field's bound for targetRatio[f] within `tolerance` by real
+ * compress passes of the plan (mlp NULL: plain bisection; else prediction,
+ * one re-targeted prediction, then bisection), leaving the chosen streams in
+ * the fields' buffers.  Outputs per field: bound, achieved ratio, passes. */
+int SZxG_batch_fixed_rate(SZxG_Batch* batch, const SZxG_Mlp* mlp, const float* targetRatio, float tolerance,
+                          int maxPasses, float* eb, float* ratio, int* passes, SZxG_StreamInfo* d_info,
+                          void* stream);
+
 /* Launch tracing: CUDA events around every kernel this library enqueues.
  * enable(1) starts (and clears) a trace, enable(0) stops and clears it.
  * collect() waits for the recorded events and writes, per kernel name, the

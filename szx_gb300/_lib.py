@@ -86,6 +86,37 @@ def _declare(L: C.CDLL) -> None:
     L.SZxG_trace_collect.restype = C.c_int
     L.SZxG_trace_collect.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(C.c_double), C.POINTER(C.c_ulonglong),
                                      C.c_int]
+    vp, ip, fp = C.c_void_p, C.POINTER(C.c_int), c_float_p
+    L.SZxG_batch_create.restype = vp
+    L.SZxG_batch_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp]
+    L.SZxG_batch_run.restype = C.c_int
+    L.SZxG_batch_run.argtypes = [vp, vp, vp]
+    L.SZxG_batch_status.restype = C.c_int
+    L.SZxG_batch_status.argtypes = [vp, vp]
+    L.SZxG_batch_destroy.restype = None
+    L.SZxG_batch_destroy.argtypes = [vp]
+    L.SZxG_batch_set_bounds.restype = C.c_int
+    L.SZxG_batch_set_bounds.argtypes = [vp, C.c_int, ip, fp, vp]
+    L.SZxG_mlp_param_count.restype = sz
+    L.SZxG_mlp_param_count.argtypes = []
+    L.SZxG_mlp_create.restype = vp
+    L.SZxG_mlp_create.argtypes = [C.c_ulonglong]
+    L.SZxG_mlp_destroy.restype = None
+    L.SZxG_mlp_destroy.argtypes = [vp]
+    L.SZxG_mlp_get_params.restype = C.c_int
+    L.SZxG_mlp_get_params.argtypes = [vp, fp, sz]
+    L.SZxG_mlp_set_params.restype = C.c_int
+    L.SZxG_mlp_set_params.argtypes = [vp, fp, sz]
+    L.SZxG_mlp_forward.restype = C.c_int
+    L.SZxG_mlp_forward.argtypes = [vp, vp, sz, vp, vp]
+    L.SZxG_mlp_gradient.restype = C.c_int
+    L.SZxG_mlp_gradient.argtypes = [vp, vp, vp, sz, vp, fp, vp]
+    L.SZxG_mlp_train.restype = C.c_int
+    L.SZxG_mlp_train.argtypes = [vp, vp, vp, sz, C.c_int, C.c_int, C.c_float, C.c_ulonglong, fp, vp]
+    L.SZxG_batch_features.restype = C.c_int
+    L.SZxG_batch_features.argtypes = [vp, C.c_int, ip, fp, vp, fp, vp]
+    L.SZxG_batch_fixed_rate.restype = C.c_int
+    L.SZxG_batch_fixed_rate.argtypes = [vp, vp, fp, C.c_float, C.c_int, fp, fp, ip, vp, vp]
     L.SZxG_decompress_host_into.restype = C.c_int
     L.SZxG_decompress_host_into.argtypes = [C.c_int, C.c_int, C.c_void_p, sz, sz, C.c_void_p]
 

@@ -19,24 +19,9 @@
 #include <vector>
 
 #include "../../include/szx_gb300.h"
-#include "kernels.h"
+#include "batch.h"
 
 using namespace szxg;
-
-struct SZxG_Batch {
-    int direction, mode, dtype, bs, nf;
-    void* dev = nullptr;
-    BlkField* d_fields = nullptr;     // device table (nf > 1)
-    BlkField one;                     // the field when nf == 1
-    StreamResult* results = nullptr;
-    unsigned long long* counters = nullptr;   // [0..3] tile counters, then the error word
-    int* err = nullptr;
-    uint8_t* zero = nullptr;          // status words and totals of every field
-    size_t zero_bytes = 0;
-    unsigned long long enc_total = 0, asm_total = 0;
-    DecField* d_dec = nullptr;        // decode: device table
-    unsigned long long idx_total = 0, dec_total = 0;
-};
 
 namespace {
 
@@ -49,7 +34,39 @@ SZxG_Batch* fail(int code) {
 
 }  // namespace
 
+cudaError_t batch_select(SZxG_Batch* b, int nActive, const int* h_idx, const float* h_eb, cudaStream_t s) {
+    if (b->direction != 0 || nActive < 1 || nActive > b->nf) return cudaErrorInvalidValue;
+    if (!h_idx && nActive != b->nf) return cudaErrorInvalidValue;
+    const size_t tb = (size_t)blocked_tile_blocks(b->dtype, b->bs);
+    std::vector<BlkField> run((size_t)nActive);
+    unsigned long long et = 0, at = 0;
+    for (int k = 0; k < nActive; k++) {
+        const int f = h_idx ? h_idx[k] : k;
+        if (f < 0 || f >= b->nf) return cudaErrorInvalidValue;
+        if (h_eb) b->tab[f].eb = h_eb[k];
+        BlkField F = b->tab[f];
+        F.enc_tiles = (F.nb + tb - 1) / tb; F.enc_tile0 = et; et += F.enc_tiles;
+        F.asm_tiles = (F.nb + kAsmBlocksPerTile - 1) / kAsmBlocksPerTile; F.asm_tile0 = at; at += F.asm_tiles;
+        run[(size_t)k] = F;
+    }
+    b->enc_total = et;
+    b->asm_total = at;
+    b->one = run[0];
+    b->nrun = nActive;
+    // pageable source: the copy is staged before the call returns, ordered after earlier runs on s
+    return cudaMemcpyAsync(b->d_fields, run.data(), sizeof(BlkField) * (size_t)nActive, cudaMemcpyHostToDevice, s);
+}
+
 extern "C" {
+
+int SZxG_batch_set_bounds(SZxG_Batch* b, int nActive, const int* fieldIndex, const float* absErrBound, void* stream) {
+    if (!b || b->direction != 0) { set_last_error(SZXG_ERR_ARG); return SZXG_ERR_ARG; }
+    cudaError_t e = batch_select(b, nActive, fieldIndex, absErrBound, (cudaStream_t)stream);
+    if (e == cudaErrorInvalidValue) { set_last_error(SZXG_ERR_ARG); return SZXG_ERR_ARG; }
+    if (e != cudaSuccess) { cudaGetLastError(); set_last_error(SZXG_ERR_CUDA); return SZXG_ERR_CUDA; }
+    set_last_error(SZXG_OK);
+    return SZXG_OK;
+}
 
 static SZxG_Batch* create_decode(int fastMode, int dataType, int blockSize, int nFields, const SZxG_Field* fields) {
     if (fastMode != kRandomAccess && fastMode != kRandomAccessNative) return fail(SZXG_ERR_UNSUPPORTED);
@@ -202,6 +219,8 @@ SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blo
     b->enc_total = et;
     b->asm_total = at;
     b->one = tab[0];
+    b->tab = tab;
+    b->nrun = nFields;
     b->d_fields = (BlkField*)(base + o_tab);
     if (cudaMemcpy(b->d_fields, tab.data(), sizeof(BlkField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaGetLastError();
@@ -222,7 +241,7 @@ int SZxG_batch_run(SZxG_Batch* b, SZxG_StreamInfo* d_info, void* stream) {
         e = launch_blocked_decode_fields(b->mode, b->dtype, b->bs, b->nf, b->d_dec, b->idx_total, b->dec_total,
                                          b->counters, b->results, b->err, s);
     else if (e == cudaSuccess)
-        e = launch_blocked_encode_fields(b->mode, b->dtype, b->bs, b->nf, b->one, b->nf > 1 ? b->d_fields : nullptr,
+        e = launch_blocked_encode_fields(b->mode, b->dtype, b->bs, b->nrun, b->one, b->nrun > 1 ? b->d_fields : nullptr,
                                          b->enc_total, b->asm_total, b->counters, b->err, s);
     if (e == cudaSuccess && d_info)
         e = cudaMemcpyAsync(d_info, b->results, sizeof(StreamResult) * b->nf, cudaMemcpyDeviceToDevice, s);
@@ -249,6 +268,7 @@ int SZxG_batch_status(SZxG_Batch* b, void* stream) {
 
 void SZxG_batch_destroy(SZxG_Batch* b) {
     if (!b) return;
+    lfx_free(b->lfx);
     if (b->dev) cudaFree(b->dev);
     delete b;
 }
