@@ -53,8 +53,14 @@ cudaError_t batch_select(SZxG_Batch* b, int nActive, const int* h_idx, const flo
     b->asm_total = at;
     b->one = run[0];
     b->nrun = nActive;
-    // pageable source: the copy is staged before the call returns, ordered after earlier runs on s
-    return cudaMemcpyAsync(b->d_fields, run.data(), sizeof(BlkField) * (size_t)nActive, cudaMemcpyHostToDevice, s);
+    // pageable sources: each copy is staged before the call returns, ordered after earlier runs on s
+    cudaError_t e = cudaMemcpyAsync(b->d_fields, run.data(), sizeof(BlkField) * (size_t)nActive,
+                                    cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess || nActive == 1) return e;
+    b->h_tile_field.resize(et);
+    for (int k = 0; k < nActive; k++)
+        for (unsigned long long t = 0; t < run[(size_t)k].enc_tiles; t++) b->h_tile_field[run[(size_t)k].enc_tile0 + t] = (uint32_t)k;
+    return cudaMemcpyAsync(b->d_tile_field, b->h_tile_field.data(), 4 * et, cudaMemcpyHostToDevice, s);
 }
 
 extern "C" {
@@ -79,6 +85,9 @@ static SZxG_Batch* create_decode(int fastMode, int dataType, int blockSize, int 
     const size_t o_res = off; off += a256(sizeof(StreamResult) * nf);
     const size_t o_ctr = off; off += 256;
     const size_t o_hdr = off; off += a256(sizeof(BlockedHdr) * nf);
+    unsigned long long dec_tiles_all = 0;
+    for (size_t f = 0; f < nf; f++) dec_tiles_all += ((fields[f].nbEle + blockSize - 1) / blockSize + tb - 1) / tb;
+    const size_t o_map = off; off += a256(4 * dec_tiles_all);
     const size_t o_zero = off;
     const size_t o_err = off; off += a256(sizeof(int) * nf);
     std::vector<size_t> o_st(nf), o_p(nf), o_rw(nf), ta(nf), tbw(nf);
@@ -135,7 +144,12 @@ static SZxG_Batch* create_decode(int fastMode, int dataType, int blockSize, int 
     b->idx_total = it;
     b->dec_total = dt;
     b->d_dec = (DecField*)(base + o_tab);
-    if (cudaMemcpy(b->d_dec, tab.data(), sizeof(DecField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
+    b->d_tile_field = (uint32_t*)(base + o_map);
+    b->h_tile_field.resize(dt);
+    for (size_t f = 0; f < nf; f++)
+        for (unsigned long long t = 0; t < tab[f].dec_tiles; t++) b->h_tile_field[tab[f].dec_tile0 + t] = (uint32_t)f;
+    if (cudaMemcpy(b->d_tile_field, b->h_tile_field.data(), 4 * dt, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->d_dec, tab.data(), sizeof(DecField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(b->dev);
         delete b;
@@ -161,6 +175,10 @@ SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blo
     const size_t o_tab = off; off += a256(sizeof(BlkField) * nf);
     const size_t o_res = off; off += a256(sizeof(StreamResult) * nf);
     const size_t o_ctr = off; off += 256;
+    unsigned long long tiles_all = 0;
+    for (size_t f = 0; f < nf; f++)
+        tiles_all += ((fields[f].nbEle + blockSize - 1) / blockSize + tb - 1) / tb;
+    const size_t o_map = off; off += a256(4 * tiles_all);
     const size_t o_zero = off;
     std::vector<size_t> o_st(nf), o_tot(nf), o_sz(nf), o_md(nf), o_ss(nf);
     for (size_t f = 0; f < nf; f++) {
@@ -222,7 +240,12 @@ SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blo
     b->tab = tab;
     b->nrun = nFields;
     b->d_fields = (BlkField*)(base + o_tab);
-    if (cudaMemcpy(b->d_fields, tab.data(), sizeof(BlkField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
+    b->d_tile_field = (uint32_t*)(base + o_map);
+    b->h_tile_field.resize(et);
+    for (size_t f = 0; f < nf; f++)
+        for (unsigned long long t = 0; t < tab[f].enc_tiles; t++) b->h_tile_field[tab[f].enc_tile0 + t] = (uint32_t)f;
+    if (cudaMemcpy(b->d_tile_field, b->h_tile_field.data(), 4 * et, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->d_fields, tab.data(), sizeof(BlkField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(b->dev);
         delete b;
@@ -238,11 +261,12 @@ int SZxG_batch_run(SZxG_Batch* b, SZxG_StreamInfo* d_info, void* stream) {
     cudaError_t e = cudaMemsetAsync(b->zero, 0, b->zero_bytes, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->counters, 0, 128, s);
     if (e == cudaSuccess && b->direction == 1)
-        e = launch_blocked_decode_fields(b->mode, b->dtype, b->bs, b->nf, b->d_dec, b->idx_total, b->dec_total,
+        e = launch_blocked_decode_fields(b->mode, b->dtype, b->bs, b->nf, b->d_dec, b->d_tile_field, b->idx_total,
+                                         b->dec_total,
                                          b->counters, b->results, b->err, s);
     else if (e == cudaSuccess)
         e = launch_blocked_encode_fields(b->mode, b->dtype, b->bs, b->nrun, b->one, b->nrun > 1 ? b->d_fields : nullptr,
-                                         b->enc_total, b->asm_total, b->counters, b->err, s);
+                                         b->d_tile_field, b->enc_total, b->asm_total, b->counters, b->err, s);
     if (e == cudaSuccess && d_info)
         e = cudaMemcpyAsync(d_info, b->results, sizeof(StreamResult) * b->nf, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) {

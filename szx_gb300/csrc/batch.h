@@ -27,6 +27,8 @@ struct SZxG_Batch {
     // compress: every field's table entry (host copy) and how many a run codes
     std::vector<BlkField> tab;
     int nrun = 0;
+    uint32_t* d_tile_field = nullptr;   // field (index into the run's table) of every encode tile
+    std::vector<uint32_t> h_tile_field;
     LfxWork* lfx = nullptr;
 };
 

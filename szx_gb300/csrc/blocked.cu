@@ -67,6 +67,7 @@ struct EncArgs {
     int omp_stats;               // mode-4 double statistics
     unsigned long long total_tiles;
     unsigned long long* tile_ctr;
+    const uint32_t* tile_field;  // nf > 1: field of every launch-wide tile
     int* err;
 };
 
@@ -290,16 +291,8 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     const long long nt = (long long)a.total_tiles;
     const unsigned long long tile_elems = (unsigned long long)TB * a.bs;
     const bool vec = ((a.bs * (int)sizeof(T)) & 15) == 0;   // every block starts 16-byte aligned
-    // field of a launch-wide tile (fields in ascending enc_tile0)
-    auto field_of = [&](long long g) {
-        int lo = 0, hi = a.nf - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if ((long long)a.fields[mid].enc_tile0 <= g) lo = mid;
-            else hi = mid - 1;
-        }
-        return lo;
-    };
+    // field of a launch-wide tile: one load from the plan's tile map
+    auto field_of = [&](long long g) { return (int)a.tile_field[g]; };
     if (threadIdx.x == 0) {
         for (int i = 0; i < 2; i++) mbar_init(&bar[i], 1);
         mbar_fence_init();
@@ -686,10 +679,10 @@ int blocked_tile_blocks(int dtype, int bs) {
 }
 
 cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, const BlkField& one,
-                                         const BlkField* d_fields, unsigned long long enc_total,
-                                         unsigned long long asm_total, unsigned long long* counters, int* err,
-                                         cudaStream_t s) {
-    if (nf < 1 || enc_total == 0) return cudaErrorInvalidValue;
+                                         const BlkField* d_fields, const uint32_t* d_tile_field,
+                                         unsigned long long enc_total, unsigned long long asm_total,
+                                         unsigned long long* counters, int* err, cudaStream_t s) {
+    if (nf < 1 || enc_total == 0 || (nf > 1 && !d_tile_field)) return cudaErrorInvalidValue;
     EncArgs a;
     a.one = one;
     a.fields = d_fields;
@@ -698,6 +691,7 @@ cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, 
     a.omp_stats = layout == kRandomAccessNative;
     a.total_tiles = enc_total;
     a.tile_ctr = &counters[0];
+    a.tile_field = d_tile_field;
     a.err = err;
     cudaError_t e;
     const int G = lanes_for_bs(dtype, bs);
@@ -763,8 +757,8 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
     F.size_blk = ws.o_scr; F.med_blk = ws.m_scr; F.s_scr = ws.s_scr;
     F.tot = ws.totals;
     F.res = ws.result;
-    return launch_blocked_encode_fields(layout, dtype, bs, 1, F, nullptr, F.enc_tiles, F.asm_tiles, ws.counters,
-                                        ws.err, s);
+    return launch_blocked_encode_fields(layout, dtype, bs, 1, F, nullptr, nullptr, F.enc_tiles, F.asm_tiles,
+                                        ws.counters, ws.err, s);
 }
 
 // ------------------------------------------------------------------ decode
@@ -1143,6 +1137,7 @@ struct DecArgs {
     int native_medians;
     int* err;                      // one stream: its error word; a batch: the launch's (bounded waits)
     const DecField* fields;        // a batch: the field table (ascending dec_tile0), else unused
+    const uint32_t* tile_field;    // a batch: field of every launch-wide decode tile
     int nf, bs;
     unsigned long long total_tiles;
 };
@@ -1183,16 +1178,8 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
     __syncthreads();
     const long long ntiles = MULTI ? (long long)a.total_tiles : (long long)((h.nb + TB - 1) / TB);
     const int bs = MULTI ? a.bs : (int)h.bs;
-    // field of a launch-wide tile (batch)
-    auto field_of = [&](long long g) {
-        int lo = 0, hi = a.nf - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if ((long long)a.fields[mid].dec_tile0 <= g) lo = mid;
-            else hi = mid - 1;
-        }
-        return lo;
-    };
+    // field of a launch-wide tile (batch): one load from the plan's tile map
+    auto field_of = [&](long long g) { return (int)a.tile_field[g]; };
 
     if (warp == kDecWarps) {
         // ---------------------------------------------------------- producer
@@ -1403,8 +1390,8 @@ static cudaError_t run_decode(const uint8_t* s, size_t len, size_t nb, const Wor
 }
 
 template <typename T, int G>
-static cudaError_t run_decode_fields(const DecField* F, int nf, int bs, unsigned long long total, int native,
-                                     int* lerr, cudaStream_t st) {
+static cudaError_t run_decode_fields(const DecField* F, const uint32_t* tf, int nf, int bs, unsigned long long total,
+                                     int native, int* lerr, cudaStream_t st) {
     using TL = DecTileV<T, G>;
     cudaError_t e = dec_attr<T, G, true>();
     if (e != cudaSuccess) return e;
@@ -1412,7 +1399,7 @@ static cudaError_t run_decode_fields(const DecField* F, int nf, int bs, unsigned
     const int grid = (int)(total < cap ? (total ? total : 1) : cap);
     DecArgs a = {};
     a.native_medians = native; a.err = lerr;
-    a.fields = F; a.nf = nf; a.bs = bs; a.total_tiles = total;
+    a.fields = F; a.tile_field = tf; a.nf = nf; a.bs = bs; a.total_tiles = total;
     TraceScope tr("blocked_decode_fields", st);
     k_blocked_decode<T, G, true><<<grid, kDecThreadsP, TL::kDynSmem, st>>>(a);
     return cudaGetLastError();
@@ -1446,7 +1433,8 @@ __global__ void k_blocked_decode_finish(const DecField* F, int nf, int esize, St
 }
 
 cudaError_t launch_blocked_decode_fields(int layout, int dtype, int bs, int nf, const DecField* d_fields,
-                                         unsigned long long idx_total, unsigned long long dec_total,
+                                         const uint32_t* d_tile_field, unsigned long long idx_total,
+                                         unsigned long long dec_total,
                                          unsigned long long* counters, StreamResult* res, int* err,
                                          cudaStream_t s) {
     if (layout != kRandomAccess && layout != kRandomAccessNative) return cudaErrorInvalidValue;
@@ -1466,20 +1454,20 @@ cudaError_t launch_blocked_decode_fields(int layout, int dtype, int bs, int nf, 
     cudaError_t e;
     if (dtype == 0) {
         switch (dec_lanes(dtype, bs)) {
-            case 1: e = run_decode_fields<float, 1>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            case 2: e = run_decode_fields<float, 2>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            case 4: e = run_decode_fields<float, 4>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            case 8: e = run_decode_fields<float, 8>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            default: e = run_decode_fields<float, 16>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 1: e = run_decode_fields<float, 1>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 2: e = run_decode_fields<float, 2>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 4: e = run_decode_fields<float, 4>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 8: e = run_decode_fields<float, 8>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            default: e = run_decode_fields<float, 16>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
         }
     } else {
         switch (dec_lanes(dtype, bs)) {
-            case 1: e = run_decode_fields<double, 1>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            case 2: e = run_decode_fields<double, 2>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            case 4: e = run_decode_fields<double, 4>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            case 8: e = run_decode_fields<double, 8>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            case 16: e = run_decode_fields<double, 16>(d_fields, nf, bs, dec_total, native, lerr, s); break;
-            default: e = run_decode_fields<double, 32>(d_fields, nf, bs, dec_total, native, lerr, s); break;
+            case 1: e = run_decode_fields<double, 1>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 2: e = run_decode_fields<double, 2>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 4: e = run_decode_fields<double, 4>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 8: e = run_decode_fields<double, 8>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 16: e = run_decode_fields<double, 16>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            default: e = run_decode_fields<double, 32>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
         }
     }
     if (e != cudaSuccess) return e;

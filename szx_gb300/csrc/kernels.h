@@ -192,23 +192,26 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
                                   float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s);
 // Blocks per encode tile for this type and block size (tile counts of a
 // field table), and the encode + assemble of nf fields in one launch each:
-// `one` when nf == 1, else the device table d_fields (ascending tile starts);
+// `one` when nf == 1, else the device table d_fields (ascending tile starts)
+// with d_tile_field[g] = the field of launch-wide encode tile g;
 // counters[0..2] and err zeroed by the caller, like every field's status
 // words and totals.
 int blocked_tile_blocks(int dtype, int bs);
 cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, const BlkField& one,
-                                         const BlkField* d_fields, unsigned long long enc_total,
-                                         unsigned long long asm_total, unsigned long long* counters, int* err,
-                                         cudaStream_t s);
+                                         const BlkField* d_fields, const uint32_t* d_tile_field,
+                                         unsigned long long enc_total, unsigned long long asm_total,
+                                         unsigned long long* counters, int* err, cudaStream_t s);
 // Blocked decode of nf streams (layouts 3, 4) in one launch per kernel: the
 // headers are parsed into the fields' hdr, counters[0] and every field's
 // look-back words and error word zeroed by the caller; res[f] receives field
 // f's outcome and *err the first failing status.  idx_total / dec_total: the
-// launch-wide index and decode tiles (sums over the table).
+// launch-wide index and decode tiles (sums over the table); d_tile_field[g]:
+// the field of launch-wide decode tile g.
 int blocked_dec_tile_blocks(int dtype, int bs);
 constexpr unsigned long long kIdxPerTile = 2048;   // items per tile of the index scans
 cudaError_t launch_blocked_decode_fields(int layout, int dtype, int bs, int nf, const DecField* d_fields,
-                                         unsigned long long idx_total, unsigned long long dec_total,
+                                         const uint32_t* d_tile_field, unsigned long long idx_total,
+                                         unsigned long long dec_total,
                                          unsigned long long* counters, StreamResult* res, int* err,
                                          cudaStream_t s);
 // Blocked decode (layouts 3, 4).
