@@ -1,4 +1,5 @@
-"""Build recipe for libszx_gb300.so (CUDA kernels + C ABI) for sm_103a.
+"""Build recipe for libszx_gb300.so (CUDA kernels + C ABI) for sm_103a, and
+the `szx` command-line tool (bin/szx) on top of it.
 
 Each translation unit in csrc/ is compiled in parallel by nvcc with one
 -gencode (compute_103a -> sm_103a), FMA contraction off (the reference does
@@ -37,7 +38,7 @@ def sources() -> list[str]:
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    deps.append(os.path.join(os.path.dirname(PKG), "include", "szx_gb300.h"))
+    deps += [os.path.join(os.path.dirname(PKG), "include", h) for h in ("szx_gb300.h", "szx_rw.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps if os.path.exists(d)):
         return obj
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
@@ -56,15 +57,38 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
-    if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+    if not (os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs)):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print("built", LIB)
+    build_cli(verbose)
+    return LIB
+
+
+CLI_SRC = os.path.join(PKG, "cli", "szx.cpp")
+CLI = os.path.join(PKG, "bin", "szx")
+
+
+def build_cli(verbose: bool = False) -> str:
+    """The `szx` command-line tool, linked against libszx_gb300.so (found next
+    to bin/ through its rpath)."""
+    inc = os.path.join(os.path.dirname(PKG), "include")
+    deps = [CLI_SRC, LIB, os.path.join(inc, "szx_gb300.h"), os.path.join(inc, "szx_rw.h")]
+    if os.path.exists(CLI) and all(os.path.getmtime(CLI) >= os.path.getmtime(d) for d in deps):
+        return CLI
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", CLI_SRC, "-o", CLI, "-L" + PKG, "-lszx_gb300", "-lm",
+           "-Wl,-rpath,$ORIGIN/.."]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        raise RuntimeError(f"building the szx tool failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", CLI)
+    return CLI
 
 
 if __name__ == "__main__":
