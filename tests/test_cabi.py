@@ -1,5 +1,6 @@
 """The C-ABI library: it loads without a GPU, exports every symbol the public
-header declares, and its host-only helpers behave like the reference's."""
+headers (include/*.h) declare, and its host-only helpers behave like the
+reference's."""
 import ctypes as C
 import os
 import re
@@ -7,7 +8,8 @@ import re
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADER = os.path.join(ROOT, "include", "szx_gb300.h")
+INCLUDE = os.path.join(ROOT, "include")
+HEADERS = sorted(os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h"))
 
 
 @pytest.fixture(scope="module")
@@ -18,11 +20,18 @@ def L():
     return lib()
 
 
+def _text():
+    return re.sub(r"/\*.*?\*/", "", "\n".join(open(h).read() for h in HEADERS), flags=re.S)
+
+
 def declared_functions():
-    text = open(HEADER).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{]*\)\s*;", text)
+    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{]*\)\s*;", _text())
     return sorted({n for n in names if n not in ("if", "sizeof")})
+
+
+def declared_variables():
+    return sorted(set(re.findall(r"^\s*extern\s+[A-Za-z_][A-Za-z0-9_ ]*?\b([A-Za-z_][A-Za-z0-9_]*)\s*;", _text(),
+                                 flags=re.M)))
 
 
 def test_header_declares_the_reference_entry_points():
@@ -39,8 +48,8 @@ def test_header_declares_the_reference_entry_points():
 
 
 def test_library_exports_every_declared_symbol(L):
-    names = declared_functions()
-    assert len(names) > 20
+    names = declared_functions() + declared_variables()
+    assert len(names) > 20 and "SZx_readFloatData" in names and "dataEndianType" in names
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
 
