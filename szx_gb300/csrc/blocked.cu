@@ -1220,7 +1220,7 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
                 word = (word << 8) | (bi < hh.sb ? (uint32_t)S[hh.s_off + bi] : 0u);
             }
             const unsigned long long rank0 = hh.ok ? RW[w] + (bit0 ? __popc(word >> (32 - bit0)) : 0) : 0;
-            // state of every block; medians of the constant ones
+            // state of every block (loads independent of the rank above)
             uint32_t ok = 1, running = 0;
             for (int j = 0; j < TB; j += 32) {
                 const int lb = j + lane;
@@ -1231,56 +1231,22 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
                 const uint32_t r = running + __popc(m & ((1u << lane) - 1));
                 running += __popc(m);
                 if (lb < TB) {
-                    if (!in) {
-                        s_kind[slot][lb] = kBlkNone;
-                    } else if (coded) {
-                        s_kind[slot][lb] = kBlkCoded;
-                        s_rank[lb] = (uint16_t)r;
-                    } else {
-                        const unsigned long long mo = hh.m_off + 4 * (b - (rank0 + r));
-                        uint32_t mbits = 0;
-                        if (b >= rank0 + r && mo + 4 <= hh.q_off) {
-                            const uint8_t* mp = S + mo;
-                            mbits = a.native_medians
-                                        ? ((uint32_t)mp[0] | ((uint32_t)mp[1] << 8) | ((uint32_t)mp[2] << 16) |
-                                           ((uint32_t)mp[3] << 24))
-                                        : (((uint32_t)mp[0] << 24) | ((uint32_t)mp[1] << 16) |
-                                           ((uint32_t)mp[2] << 8) | mp[3]);
-                        } else {
-                            ok = 0;
-                        }
-                        s_info[slot][lb] = mbits;
-                        s_kind[slot][lb] = kBlkConst;
-                    }
+                    s_kind[slot][lb] = !in ? kBlkNone : (coded ? kBlkCoded : kBlkConst);
+                    s_rank[lb] = (uint16_t)r;   // coded: rank among the tile's coded blocks; else among them before
                 }
             }
             const uint32_t nnc_t = running;
+            // the tile's payload range, then its copy at once: the rest of the
+            // metadata is gathered while the copy is in flight
             unsigned long long pa = 0, pb = 0;
             if (rank0 + nnc_t > hh.nnc) ok = 0;
-            if (__all_sync(0xffffffffu, ok) && nnc_t) {
+            if (ok && nnc_t) {
                 pa = P[rank0];
                 pb = P[rank0 + nnc_t];
                 if (pb < pa || pb - pa > (unsigned long long)TB * TL::kMaxPay || hh.q_off + pb > L) ok = 0;
             }
-            __syncwarp();
             const uint8_t* src = S + hh.q_off + pa;
             const uint32_t ph = (uint32_t)((uintptr_t)src & 15);
-            if (__all_sync(0xffffffffu, ok) && nnc_t) {
-                for (int j = 0; j < TB; j += 32) {
-                    const int lb = j + lane;
-                    if (lb < nblk && s_kind[slot][lb] == kBlkCoded) {
-                        const unsigned long long k = rank0 + s_rank[lb];
-                        const unsigned long long p0 = P[k], p1 = P[k + 1];
-                        const unsigned long long rem = hh.n - (b0 + lb) * hh.bs;
-                        const int blen = rem < hh.bs ? (int)rem : bs;
-                        const unsigned long long minsz = 5 + (unsigned long long)((blen + 3) / 4);
-                        if (p0 < pa || p1 > pb || p1 < p0 + minsz || p1 - p0 > (unsigned long long)TL::kMaxPay) ok = 0;
-                        s_info[slot][lb] = ph + (uint32_t)(p0 - pa);
-                    }
-                }
-            }
-            ok = __all_sync(0xffffffffu, ok);
-            // the payload range: aligned interior by TMA, ragged ends by the lanes
             const unsigned long long nbytes = ok ? pb - pa : 0;
             const uintptr_t sa = (uintptr_t)src;
             const uintptr_t a0 = (sa + 15) & ~(uintptr_t)15, a1 = (sa + nbytes) & ~(uintptr_t)15;
@@ -1291,6 +1257,46 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
                 head_end = a0;
                 tail_beg = a1;
             }
+            __syncwarp();
+            if (lane == 0 && tx) {
+                fence_proxy_async();
+                mbar_expect_tx(&full[slot], tx);
+                tma_load_1d(stage + ph + (a0 - sa), (const void*)a0, tx, &full[slot]);
+            }
+            // medians of the constant blocks, payload offsets of the coded ones
+            for (int j = 0; j < TB; j += 32) {
+                const int lb = j + lane;
+                if (lb >= nblk) continue;
+                const unsigned long long b = b0 + lb;
+                const uint32_t r = s_rank[lb];
+                if (s_kind[slot][lb] == kBlkConst) {
+                    const unsigned long long mo = hh.m_off + 4 * (b - (rank0 + r));
+                    uint32_t mbits = 0;
+                    if (b >= rank0 + r && mo + 4 <= hh.q_off) {
+                        const uint8_t* mp = S + mo;
+                        mbits = a.native_medians
+                                    ? ((uint32_t)mp[0] | ((uint32_t)mp[1] << 8) | ((uint32_t)mp[2] << 16) |
+                                       ((uint32_t)mp[3] << 24))
+                                    : (((uint32_t)mp[0] << 24) | ((uint32_t)mp[1] << 16) | ((uint32_t)mp[2] << 8) |
+                                       mp[3]);
+                    } else {
+                        ok = 0;
+                    }
+                    s_info[slot][lb] = mbits;
+                } else if (nbytes) {
+                    const unsigned long long k = rank0 + r;
+                    const unsigned long long p0 = P[k], p1 = P[k + 1];
+                    const unsigned long long rem = hh.n - b * hh.bs;
+                    const int blen = rem < hh.bs ? (int)rem : bs;
+                    const unsigned long long minsz = 5 + (unsigned long long)((blen + 3) / 4);
+                    if (p0 < pa || p1 > pb || p1 < p0 + minsz || p1 - p0 > (unsigned long long)TL::kMaxPay) ok = 0;
+                    s_info[slot][lb] = ph + (uint32_t)(p0 - pa);
+                } else {
+                    ok = 0;   // a coded block without a valid payload range
+                }
+            }
+            ok = __all_sync(0xffffffffu, ok);
+            // ragged ends of the payload range by the lanes
             for (uintptr_t x = sa + lane; x < head_end; x += 32) stage[ph + (x - sa)] = *(const uint8_t*)x;
             for (uintptr_t x = tail_beg + lane; x < sa + nbytes; x += 32) stage[ph + (x - sa)] = *(const uint8_t*)x;
             __threadfence_block();
@@ -1298,9 +1304,7 @@ __global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
             if (lane == 0) {
                 s_ok[slot] = (uint8_t)ok;
                 if (!ok) atomicExch(ferr, kErrStream);
-                fence_proxy_async();
-                mbar_arrive_expect_tx(&full[slot], tx);
-                if (tx) tma_load_1d(stage + ph + (a0 - sa), (const void*)a0, tx, &full[slot]);
+                mbar_arrive(&full[slot]);
             }
         }
         // copies still in flight finish before the CTA exits
