@@ -54,6 +54,12 @@ def lib() -> C.CDLL:
         L.orc_block_stats.restype = C.c_size_t
         L.orc_block_stats.argtypes = [C.c_int, C.c_void_p, C.c_size_t, C.c_float, C.c_int, C.c_void_p,
                                       C.c_void_p, C.c_void_p]
+        L.orc_cusz_bound.restype = C.c_size_t
+        L.orc_cusz_bound.argtypes = [C.c_size_t, C.c_int]
+        L.orc_cusz_compress.restype = C.c_size_t
+        L.orc_cusz_compress.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_int, C.c_void_p]
+        L.orc_cusz_decompress.restype = C.c_int
+        L.orc_cusz_decompress.argtypes = [C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p]
         L.orc_compress_m3_omp.restype = C.c_size_t
         L.orc_compress_m3_omp.argtypes = [C.c_int, C.c_void_p, C.c_size_t, C.c_float, C.c_int, C.c_void_p,
                                           C.c_size_t, C.c_int]
@@ -258,3 +264,19 @@ def ref_fxr_estimate(x: np.ndarray, eb: float, bs: int = 128):
     a, b, r = C.c_size_t(), C.c_size_t(), C.c_float()
     cr = reference().ref_fxr_estimate(_dt(x), _ptr(x), x.size, bs, eb, C.byref(a), C.byref(b), C.byref(r))
     return cr, a.value, b.value, r.value
+
+
+def cusz_compress(x: np.ndarray, eb: float, bs: int) -> bytes:
+    """The cuSZx float stream of x (cuszx_oracle.c)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty(lib().orc_cusz_bound(x.size, bs), np.uint8)
+    n = lib().orc_cusz_compress(_ptr(x), x.size, eb, bs, _ptr(out))
+    return out[:n].tobytes()
+
+
+def cusz_decompress(stream: bytes, n: int) -> np.ndarray:
+    s = np.frombuffer(stream, np.uint8).copy()
+    y = np.zeros(n, np.float32)
+    if lib().orc_cusz_decompress(_ptr(s), s.size, n, _ptr(y)) != 0:
+        raise ValueError("oracle: malformed cuSZx stream")
+    return y

@@ -38,7 +38,7 @@ def sources() -> list[str]:
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    deps += [os.path.join(os.path.dirname(PKG), "include", h) for h in ("szx_gb300.h", "szx_rw.h")]
+    deps += [os.path.join(os.path.dirname(PKG), "include", h) for h in ("szx_gb300.h", "szx_rw.h", "cuszx_entry.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps if os.path.exists(d)):
         return obj
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
