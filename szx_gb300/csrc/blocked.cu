@@ -422,17 +422,21 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
             const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
             if (in0) s_loc[slot][lane] = i0 - sz0;
             if (in1) s_loc[slot][lane + 32] = i1 - sz1;
-            if (lane == 0) {
-                s_agg[slot] = agg;
-                const long long gn = (long long)atomicAdd(a.tile_ctr, 1ull);   // this buffer's next tile
+            if (lane == 0) s_agg[slot] = agg;
+            prefix_publish(FV(F, st_enc), t, agg);
+        } else {
+            // the last warp takes this buffer's next tile (the counter's latency
+            // overlaps the zeroing and warp 0's scan); all zero this tile's
+            // staging for the spliced emission
+            const bool taker = warp == kEncWarps - 1 && lane == 0;
+            long long gn = 0;
+            if (taker) gn = (long long)atomicAdd(a.tile_ctr, 1ull);
+            uint4* z = (uint4*)(stgb + slot * TL::kStage);
+            for (int j = threadIdx.x - 32; j < TL::kStage / 16; j += kEncThreads - 32) z[j] = make_uint4(0, 0, 0, 0);
+            if (taker) {
                 s_tile[slot] = gn;
                 s_fld[slot] = (MULTI && gn < nt) ? field_of(gn) : 0;
             }
-            prefix_publish(FV(F, st_enc), t, agg);
-        } else {
-            // zero this tile's staging for the spliced emission
-            uint4* z = (uint4*)(stgb + slot * TL::kStage);
-            for (int j = threadIdx.x - 32; j < TL::kStage / 16; j += kEncThreads - 32) z[j] = make_uint4(0, 0, 0, 0);
         }
         __syncthreads();
         {

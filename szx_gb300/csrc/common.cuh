@@ -335,11 +335,11 @@ struct TileStatus32 {
 constexpr uint32_t kSt32Agg = 1u << 30, kSt32Inc = 2u << 30;
 
 __device__ __forceinline__ void st_volatile32(uint32_t* p, uint32_t v) {
-    asm volatile("st.volatile.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ uint4 ld_volatile_v4(const uint32_t* p) {
     uint4 v;
-    asm volatile("ld.volatile.global.v4.u32 {%0,%1,%2,%3}, [%4];"
+    asm volatile("ld.relaxed.gpu.global.v4.u32 {%0,%1,%2,%3}, [%4];"
                  : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
                  : "l"(p)
                  : "memory");
@@ -553,13 +553,16 @@ __device__ __forceinline__ void lookback_resolve(TileStatus32 s, long long tile,
 // of 128 predecessors (4 words per lane), with no second load for the prefix.
 constexpr unsigned long long kS64Agg = 1ull << 62, kS64Inc = 2ull << 62, kS64Val = (1ull << 62) - 1;
 
+// Status words are read and written with relaxed GPU-scope accesses: every
+// party is on this GPU, and system scope (what `volatile` means) costs far
+// more on a coherent CPU-GPU node.
 __device__ __forceinline__ void st_volatile64(unsigned long long* p, unsigned long long v) {
-    asm volatile("st.volatile.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ void ld_volatile_v2x2(const unsigned long long* p, unsigned long long (&w)[4]) {
     unsigned long long a, b, c, d;
-    asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
-    asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(c), "=l"(d) : "l"(p + 2) : "memory");
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0,%1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0,%1}, [%2];" : "=l"(c), "=l"(d) : "l"(p + 2) : "memory");
     w[0] = a; w[1] = b; w[2] = c; w[3] = d;
 }
 
