@@ -111,7 +111,10 @@ template <> __device__ __forceinline__ void add_vec<double>(RangeOps<double>& a,
     a.add(v.x, i); a.add(v.y, i + 1);
 }
 
-template <typename T>
+// STREAM: the field is larger than L2, so its lines are loaded evict-first
+// (the encoder re-reads it from HBM either way); smaller fields keep the
+// default policy and stay in L2 for the encoder that follows.
+template <typename T, bool STREAM>
 __global__ void __launch_bounds__(kRangeThreads) k_range(const T* __restrict__ x, unsigned long long n, int err_mode,
                                                           float abs_eb, float rel, RangePartial* partials,
                                                           unsigned long long* counter, CodecParams* out) {
@@ -125,13 +128,12 @@ __global__ void __launch_bounds__(kRangeThreads) k_range(const T* __restrict__ x
         const unsigned long long nv = n / VN;
         const V* xv = reinterpret_cast<const V*>(x);
         unsigned long long i = tid;
-        for (; i + 3 * nthr < nv; i += 4 * nthr) {   // 4 independent loads in flight
-            V a0 = xv[i], a1 = xv[i + nthr], a2 = xv[i + 2 * nthr],
-              a3 = xv[i + 3 * nthr];
-            add_vec<T>(acc, a0, i * VN);
-            add_vec<T>(acc, a1, (i + nthr) * VN);
-            add_vec<T>(acc, a2, (i + 2 * nthr) * VN);
-            add_vec<T>(acc, a3, (i + 3 * nthr) * VN);
+        for (; i + 7 * nthr < nv; i += 8 * nthr) {   // 8 independent 16-byte loads in flight
+            V a[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) a[u] = STREAM ? __ldcs(xv + i + u * nthr) : xv[i + u * nthr];
+#pragma unroll
+            for (int u = 0; u < 8; u++) add_vec<T>(acc, a[u], (i + u * nthr) * VN);
         }
         for (; i < nv; i += nthr) add_vec<T>(acc, xv[i], i * VN);
         for (unsigned long long j = nv * VN + tid; j < n; j += nthr) acc.add(x[j], j);
@@ -221,6 +223,9 @@ __global__ void __launch_bounds__(kRangeThreads) k_range(const T* __restrict__ x
     *out = p;
 }
 
+// Fields above this size do not fit beside the encoder's working set in L2.
+constexpr size_t kStreamBytes = size_t(96) << 20;
+
 cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float abs_eb, float rel,
                          const Workspace& ws, cudaStream_t s) {
     if (n == 0) return cudaErrorInvalidValue;
@@ -233,13 +238,14 @@ cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float
     RangePartial* parts = reinterpret_cast<RangePartial*>(ws.partials);
     cudaError_t e = cudaMemsetAsync(&ws.counters[3], 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
+    const bool stream = n * es > kStreamBytes;
     TraceScope tr("range", s);
     if (dtype == 0)
-        k_range<float><<<grid, kRangeThreads, 0, s>>>((const float*)x, n, err_mode, abs_eb, rel, parts,
-                                                      &ws.counters[3], ws.params);
+        (stream ? k_range<float, true> : k_range<float, false>)<<<grid, kRangeThreads, 0, s>>>(
+            (const float*)x, n, err_mode, abs_eb, rel, parts, &ws.counters[3], ws.params);
     else
-        k_range<double><<<grid, kRangeThreads, 0, s>>>((const double*)x, n, err_mode, abs_eb, rel, parts,
-                                                       &ws.counters[3], ws.params);
+        (stream ? k_range<double, true> : k_range<double, false>)<<<grid, kRangeThreads, 0, s>>>(
+            (const double*)x, n, err_mode, abs_eb, rel, parts, &ws.counters[3], ws.params);
     return cudaGetLastError();
 }
 
