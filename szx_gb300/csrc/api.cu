@@ -200,6 +200,18 @@ static bool check_compress_args(int mode, int dtype, size_t n, int bs, int err_m
     return true;
 }
 
+// Device -> library-allocated host copy in pieces, each enqueued once the
+// prefault workers have made its pages resident.
+static cudaError_t copy_out_pieces(void* dst, const uint8_t* src, size_t len, cudaStream_t s) {
+    for (size_t lo = 0; lo < len; lo += kHostCopyPiece) {
+        const size_t m = std::min(kHostCopyPiece, len - lo);
+        host_prefault_wait(lo + m);
+        cudaError_t e = cudaMemcpyAsync((uint8_t*)dst + lo, src + lo, m, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // Host round trip: compress host values, stream back into a host buffer.
 // `out` == nullptr allocates with malloc.  Returns stream size, 0 on failure.
 static size_t host_compress(int mode, int dtype, const void* data, size_t n, int bs, int err_mode, float abs_eb,
@@ -265,13 +277,17 @@ static size_t host_compress(int mode, int dtype, const void* data, size_t n, int
     }
     if (err) { drop(); set_err(err); return 0; }
     if (own) {
+        host_prefault_limit(r.size);
+        e = copy_out_pieces(dst, (const uint8_t*)c->out.p + r.offset, r.size, s);
         host_prefault_finish(r.size);
     } else if (out_cap < r.size) {
         set_err(SZXG_ERR_CAPACITY);
         return 0;
+    } else {
+        e = cudaMemcpyAsync(dst, (uint8_t*)c->out.p + r.offset, r.size, cudaMemcpyDeviceToHost, s);
     }
-    e = cudaMemcpyAsync(dst, (uint8_t*)c->out.p + r.offset, r.size, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    const cudaError_t es2 = cudaStreamSynchronize(s);   // no copy may still target dst when it is freed
+    if (e == cudaSuccess) e = es2;
     if (e != cudaSuccess) {
         if (own) free(dst);
         cuda_fail(e);
@@ -343,18 +359,29 @@ static void* host_decompress(int mode, int dtype, const unsigned char* bytes, si
     if (cudaMemsetAsync(ws.err, 0, sizeof(int), s) != cudaSuccess) { drop(); set_err(SZXG_ERR_CUDA); return nullptr; }
     if (enqueue_decompress(mode, dtype, d_s, len, n, bs, c->out.p, ws, s)) { drop(); return nullptr; }
     int err = 0;
+    if (own) {
+        // the values follow the decode on the stream piece by piece, each as
+        // soon as its pages are in; a failed decode's copy is discarded
+        e = cudaMemcpyAsync(&err, ws.err, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = copy_out_pieces(dst, (const uint8_t*)c->out.p, n * es, s);
+        host_prefault_finish(n * es);
+        const cudaError_t es2 = cudaStreamSynchronize(s);   // no copy may still target dst when it is freed
+        if (e == cudaSuccess) e = es2;
+        if (e != cudaSuccess) { free(dst); cuda_fail(e); return nullptr; }
+        if (err) { free(dst); set_err(err); return nullptr; }
+        set_err(SZXG_OK);
+        return dst;
+    }
+    // a caller's buffer is written only once the decode has succeeded
     if ((e = cudaMemcpyAsync(&err, ws.err, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess) {
-        drop();
         cuda_fail(e);
         return nullptr;
     }
-    if (err) { drop(); set_err(err); return nullptr; }
-    if (own) host_prefault_finish(n * es);
+    if (err) { set_err(err); return nullptr; }
     e = cudaMemcpyAsync(dst, c->out.p, n * es, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
-        if (!out) free(dst);
         cuda_fail(e);
         return nullptr;
     }

@@ -139,11 +139,19 @@ constexpr size_t enc_status_words(size_t nb) { return round4(nb / 8 + 9); }
 constexpr size_t blocked_status_words(size_t nb) { return enc_status_words(nb) + round4(nb / kAsmBlocksPerTile + 9); }
 
 // Host: fault in the pages of a fresh malloc'd output buffer [p, p+n) on a
-// few worker threads, asynchronously; host_prefault_finish(m) (m <= n) waits
-// until [p, p+m) is resident, skips the rest and ends the job.  One job at a
-// time per process; every start must be paired with a finish.
+// few worker threads, asynchronously.  host_prefault_limit(m) lowers the
+// job's extent to m bytes (the rest is skipped); host_prefault_wait(h) returns
+// once [p, p+h) is resident; host_prefault_finish(m) lowers the extent, waits
+// for the workers and ends the job.  One job at a time per process; every
+// start must be paired with a finish, and the buffer must outlive it.
 void host_prefault_start(void* p, size_t n);
+void host_prefault_limit(size_t m);
+void host_prefault_wait(size_t h);
 void host_prefault_finish(size_t m);
+
+// Bytes a library-allocated host output is copied in: each piece leaves as
+// soon as its pages are resident.
+constexpr size_t kHostCopyPiece = size_t(32) << 20;
 
 // ------------------------------------------------------------------ fixed-rate search (fxr.cu)
 
