@@ -160,10 +160,11 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
     b.med_bits = state == 1 ? payload_med : __float_as_uint(median_f);
 }
 
-// Emission of one coded block into the tile's staging buffer (zero-filled):
-// header and lead bytes with byte stores, each value's stored bytes spliced
-// into the staging words with shared-memory atomicOr (a value's bytes span at
-// most two words -- three for double -- which neighbouring values may share).
+// Emission of one coded block into the tile's staging buffer: header and lead
+// bytes, then each value's stored bytes with predicated byte stores.  Every
+// byte of [loc, loc + size) is written exactly once, so the staging buffer
+// needs no clearing and no atomics (a value's bytes are contiguous, values
+// follow each other without gaps).
 template <typename T, int G, bool FULL>
 __device__ __forceinline__ void enc_block_emit(uint8_t* stg, uint32_t loc, int len, const BlockEnc<T>& b) {
     using C = Chunks<T, G>;
@@ -185,7 +186,6 @@ __device__ __forceinline__ void enc_block_emit(uint8_t* stg, uint32_t loc, int l
     split_reqlen(b.reqLength, &R, &s);
     (void)s;
     const int low = 8 * (W - R);
-    uint32_t* sw = (uint32_t*)stg;
     uint32_t before = loc + 5 + (uint32_t)Lb;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
@@ -198,21 +198,11 @@ __device__ __forceinline__ void enc_block_emit(uint8_t* stg, uint32_t loc, int l
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const uint32_t n = byte_of(b.cnt4[k], i);
-            const uint32_t q = qb + byte_of(b.pre4[k], i);
-            const uint32_t sh = q << 3;             // (q & 3) * 8 once masked by the funnel shifts
-            const uint32_t w = q >> 2, lim = (q & 3) + n;
-            if constexpr (sizeof(T) == 4) {
-                const uint32_t ev = (b.cur[4 * k + i] >> low) & __funnelshift_rc(0xFFFFFFFFu, 0u, 32 - 8 * n);
-                if (n) atomicOr(&sw[w], __funnelshift_l(0u, ev, sh));
-                if (lim > 4) atomicOr(&sw[w + 1], __funnelshift_l(ev, 0u, sh));
-            } else {
-                const unsigned long long m = n >= 8 ? ~0ull : ((1ull << (8 * n)) - 1);
-                const unsigned long long ev = (b.cur[4 * k + i] >> low) & m;
-                const uint32_t lo = (uint32_t)ev, hi = (uint32_t)(ev >> 32);
-                if (n) atomicOr(&sw[w], __funnelshift_l(0u, lo, sh));
-                if (lim > 4) atomicOr(&sw[w + 1], __funnelshift_l(lo, hi, sh));
-                if (lim > 8) atomicOr(&sw[w + 2], __funnelshift_l(hi, 0u, sh));
-            }
+            uint8_t* d = stg + qb + byte_of(b.pre4[k], i);
+            const U ev = b.cur[4 * k + i] >> low;
+#pragma unroll
+            for (int j = 0; j < W; j++)
+                if ((uint32_t)j < n) d[j] = (uint8_t)(ev >> (8 * j));
         }
     }
 }
@@ -258,16 +248,24 @@ struct EncTile {
     static constexpr int kStage = ((kBlocks * kMaxPay + 32 + 15) / 16) * 16;
     static constexpr int kDynSmem = 2 * kIn + 2 * kStage;
     static_assert(kBlocks / kBpw <= kEncWarps, "one block group per warp");
+    static_assert(kBlocks <= 64, "a tile's sizes are scanned as two warp-wide halves");
+    static_assert(kIn % 16 == 0 && kStage % 16 == 0, "TMA destinations stay 16-byte aligned");
 };
 
 // One pass over the input.  Per tile t_i (double-buffered input by TMA,
-// double-buffered staging):
-//   statistics of every block (registers)  ->  tile scan, publish t_i's byte
-//   count  ->  emission of t_i into zeroed staging  ->  look-back of t_{i-1}
-//   ->  copy-out of t_{i-1} to its place in the payload region.
-// A segment of G lanes owns one block from its statistics to its emission;
-// the look-back of a tile runs one tile later than its publication, so
-// predecessors have normally published by then.
+// double-buffered staging), three CTA barriers:
+//   statistics of every block (registers)  |  barrier  |  refill of the input
+//   buffer with t_{i+2}; every warp scans the tile's block sizes for its own
+//   blocks' offsets (warp 0 publishes the tile's byte count) and emits them
+//   into staging, while warp 0 also places t_{i-1} by a look-back whose first
+//   loads were issued before its emission  |  barrier  |  copy-out of t_{i-1}
+//   to its place in the payload region  |  barrier.
+// Tile ids come from an atomic counter, taken in increasing order two tiles
+// ahead (the look-back stays deadlock-free with any number of resident CTAs);
+// the counter's reply is awaited only after the statistics.  A segment of G
+// lanes owns one block from its statistics to its emission; the look-back of a
+// tile runs one tile later than its publication, so predecessors have
+// normally published by then.
 template <typename T, int G, bool MULTI>
 __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     using TL = EncTile<T, G>;
@@ -278,11 +276,13 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     uint8_t* inb = dsm;
     uint8_t* stgb = dsm + 2 * TL::kIn;
     __shared__ unsigned long long bar[2];
-    __shared__ uint32_t s_size[2][TB], s_med[2][TB], s_loc[2][TB];
+    __shared__ uint32_t s_size[2][TB], s_med[2][TB];
     __shared__ uint8_t s_state[2][TB];
     __shared__ uint32_t s_agg[2];
     __shared__ long long s_tile[2];     // launch-wide tile index held by each input buffer
     __shared__ int s_fld[2];            // its field
+    __shared__ long long s_next;        // the tile taken during the current one
+    __shared__ int s_fnext;
     __shared__ unsigned long long s_base;
     __shared__ int s_skip;
     const int warp = threadIdx.x >> 5;
@@ -312,6 +312,7 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         const unsigned long long rem = FV(F, n) - start;
         return rem < tile_elems ? rem : tile_elems;
     };
+    // all threads: TMA of the 16-byte part by thread 0, the rest by plain copies
     auto issue = [&](long long g, int f, int which) {
         const BlkField* F = fld(f);
         const long long t = g - (long long)FV(F, enc_tile0);
@@ -344,9 +345,9 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
 
     unsigned long long nnc_cta = 0;   // warp 0 lane 0, single field: non-constant blocks of this CTA's tiles
     // warp 0: offset of tile t of field F (slot), its sizes / medians / state bits by block
-    auto resolve = [&](const BlkField* F, long long t, int slot) {
+    auto resolve = [&](const BlkField* F, long long t, int slot, const LookbackWin& lw) {
         const uint32_t agg = s_agg[slot];
-        const unsigned long long base = prefix_resolve(FV(F, st_enc), t, agg, a.err);
+        const unsigned long long base = prefix_resolve_pre(FV(F, st_enc), t, agg, a.err, lw);
         const bool cap_ok = base + agg <= FV(F, payload_cap);
         const unsigned long long tb0 = (unsigned long long)t * TB;
         uint32_t m01[2];
@@ -382,6 +383,7 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         if (g0 < nt) issue(g0, s_fld[0], 0);
         if (g1 < nt) issue(g1, s_fld[1], 1);
     }
+    const bool taker = warp == kEncWarps - 1 && lane == 0;
     long long t_prev = -1;
     int f_prev = 0;
     int i = 0;
@@ -393,6 +395,9 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         const int f = s_fld[slot];
         const BlkField* F = fld(f);
         const long long t = g - (long long)FV(F, enc_tile0);
+        // the last warp takes this buffer's next tile; the reply is used after the statistics
+        unsigned long long gn = 0;
+        if (taker) gn = atomicAdd(a.tile_ctr, 1ull);
         wait_buf(F, t, slot);
         // ---- statistics of the tile's blocks, one block per segment
         const int lb = warp * BPW + seg;
@@ -411,45 +416,45 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
                 s_med[slot][lb] = b.med_bits;
             }
         }
-        __syncthreads();
-        if (warp == 0) {
-            // tile scan and publication of its byte count
-            const bool in0 = lane < TB, in1 = lane + 32 < TB;
-            const uint32_t sz0 = in0 ? s_size[slot][lane] : 0, sz1 = in1 ? s_size[slot][lane + 32] : 0;
-            const uint32_t i0 = warp_inclusive_sum(sz0);
-            const uint32_t c0 = __shfl_sync(0xffffffffu, i0, 31);
-            const uint32_t i1 = warp_inclusive_sum(sz1) + c0;
-            const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
-            if (in0) s_loc[slot][lane] = i0 - sz0;
-            if (in1) s_loc[slot][lane + 32] = i1 - sz1;
-            if (lane == 0) s_agg[slot] = agg;
-            prefix_publish(FV(F, st_enc), t, agg);
-        } else {
-            // the last warp takes this buffer's next tile (the counter's latency
-            // overlaps the zeroing and warp 0's scan); all zero this tile's
-            // staging for the spliced emission
-            const bool taker = warp == kEncWarps - 1 && lane == 0;
-            long long gn = 0;
-            if (taker) gn = (long long)atomicAdd(a.tile_ctr, 1ull);
-            uint4* z = (uint4*)(stgb + slot * TL::kStage);
-            for (int j = threadIdx.x - 32; j < TL::kStage / 16; j += kEncThreads - 32) z[j] = make_uint4(0, 0, 0, 0);
-            if (taker) {
-                s_tile[slot] = gn;
-                s_fld[slot] = (MULTI && gn < nt) ? field_of(gn) : 0;
+        if (taker) {
+            s_next = (long long)gn;
+            s_fnext = (MULTI && (long long)gn < nt) ? field_of((long long)gn) : 0;
+        }
+        __syncthreads();   // statistics in, input buffer free, next tile id known
+        {
+            const long long gq = s_next;
+            const int fq = s_fnext;
+            if (gq < nt) issue(gq, fq, slot);
+            if (threadIdx.x == 0) {   // read again two tiles on, after the barriers between
+                s_tile[slot] = gq;
+                s_fld[slot] = fq;
             }
         }
-        __syncthreads();
-        {
-            const long long gn = s_tile[slot];
-            if (gn < nt) issue(gn, s_fld[slot], slot);
+        // warp 0: the previous tile's first look-back window, in flight during the emission
+        LookbackWin lw;
+        if (warp == 0 && t_prev >= 0) lookback_load(FV(fld(f_prev), st_enc), t_prev, lw);
+        // every warp: the tile's block offsets (two warp-wide halves)
+        const bool in0 = lane < TB, in1 = lane + 32 < TB;
+        const uint32_t sz0 = in0 ? s_size[slot][lane] : 0, sz1 = in1 ? s_size[slot][lane + 32] : 0;
+        const uint32_t i0 = warp_inclusive_sum(sz0);
+        const uint32_t c0 = __shfl_sync(0xffffffffu, i0, 31);
+        const uint32_t i1 = warp_inclusive_sum(sz1) + c0;
+        const uint32_t e0 = i0 - sz0, e1 = i1 - sz1;
+        const uint32_t loc_lo = __shfl_sync(0xffffffffu, e0, lb & 31);
+        const uint32_t loc_hi = __shfl_sync(0xffffffffu, e1, lb & 31);
+        if (warp == 0) {
+            const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
+            if (lane == 0) s_agg[slot] = agg;
+            prefix_publish(FV(F, st_enc), t, agg);
         }
         if (mine && b.state == 1) {
             uint8_t* stg = stgb + slot * TL::kStage;
-            if (full) enc_block_emit<T, G, true>(stg, s_loc[slot][lb], len, b);
-            else enc_block_emit<T, G, false>(stg, s_loc[slot][lb], len, b);
+            const uint32_t loc = lb < 32 ? loc_lo : loc_hi;
+            if (full) enc_block_emit<T, G, true>(stg, loc, len, b);
+            else enc_block_emit<T, G, false>(stg, loc, len, b);
         }
-        if (warp == 0 && t_prev >= 0) resolve(fld(f_prev), t_prev, slot ^ 1);
-        __syncthreads();
+        if (warp == 0 && t_prev >= 0) resolve(fld(f_prev), t_prev, slot ^ 1, lw);
+        __syncthreads();   // payloads staged, previous tile placed
         if (t_prev >= 0 && !s_skip)
             cta_copy_realign(stgb + (slot ^ 1) * TL::kStage, s_agg[slot ^ 1], FV(fld(f_prev), payload) + s_base);
         t_prev = t;
@@ -458,7 +463,11 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     // the last tile of this CTA: placed and written out after the loop
     if (t_prev >= 0) {
         const int ps = (i & 1) ^ 1;
-        if (warp == 0) resolve(fld(f_prev), t_prev, ps);
+        if (warp == 0) {
+            LookbackWin lw;
+            lookback_load(FV(fld(f_prev), st_enc), t_prev, lw);
+            resolve(fld(f_prev), t_prev, ps, lw);
+        }
         __syncthreads();
         if (!s_skip) cta_copy_realign(stgb + ps * TL::kStage, s_agg[ps], FV(fld(f_prev), payload) + s_base);
     }
@@ -636,18 +645,27 @@ template <typename T, int G>
 static cudaError_t run_encode(EncArgs a, cudaStream_t s) {
     using TL = EncTile<T, G>;
     static bool attr_set[64] = {false};
+    static int per_sm[64] = {0};
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_blocked_encode<T, G, false>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, TL::kDynSmem);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!attr_set[dev]) {
+        // the ring needs the largest shared-memory carveout for 3 CTAs per SM
+        cudaError_t e = cudaSuccess;
+        for (auto k : {k_blocked_encode<T, G, false>, k_blocked_encode<T, G, true>}) {
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TL::kDynSmem);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        }
+        int occ = 0;
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_blocked_encode<T, G, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     TL::kDynSmem);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_blocked_encode<T, G, false>, kEncThreads,
+                                                              TL::kDynSmem);
         if (e != cudaSuccess) return e;
+        per_sm[dev] = occ < 1 ? 1 : occ;
         attr_set[dev] = true;
     }
-    const size_t g = (size_t)sm_count() * 3;
+    const size_t g = (size_t)sm_count() * per_sm[dev];
     const int grid = (int)(a.total_tiles < g ? a.total_tiles : g);
     TraceScope tr("blocked_encode", s);
     if (a.nf > 1) k_blocked_encode<T, G, true><<<grid, kEncThreads, TL::kDynSmem, s>>>(a);

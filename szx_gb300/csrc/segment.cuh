@@ -94,6 +94,23 @@ __device__ __forceinline__ float fmax_nan(float a, float b) {
     asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
     return r;
 }
+// Three-input forms (sm_100 and later): NaN inputs are ignored like fminf /
+// fmaxf, or propagated like fmax_nan.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmax3_nan(float a, float b, float c) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
 // bytes [0, n) of a word set (n <= 0: none, n >= 4: all)
 __device__ __forceinline__ uint32_t low_bytes_mask(int n) {
     return n >= 4 ? 0xFFFFFFFFu : (n <= 0 ? 0u : 0xFFFFFFFFu >> (32 - 8 * n));
@@ -111,12 +128,21 @@ __device__ __forceinline__ void seg_minmax(const T (&v)[EncCfg<T>::E], int len, 
     const int sl = (int)(lane_id() & (G - 1));
     if constexpr (sizeof(T) == 4) {
         float lo = __builtin_huge_valf(), hi = -__builtin_huge_valf(), hn = -__builtin_huge_valf();
+        if constexpr (FULL) {
 #pragma unroll
-        for (int e = 0; e < E; e++) {
-            if (FULL || C::first(sl, e / 4) + (e & 3) < len) {
-                lo = fminf(lo, v[e]);
-                hi = fmaxf(hi, v[e]);
-                hn = fmax_nan(hn, v[e]);
+            for (int e = 0; e < E; e += 2) {
+                lo = fmin3(lo, v[e], v[e + 1]);
+                hi = fmax3(hi, v[e], v[e + 1]);
+                hn = fmax3_nan(hn, v[e], v[e + 1]);
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                if (C::first(sl, e / 4) + (e & 3) < len) {
+                    lo = fminf(lo, v[e]);
+                    hi = fmaxf(hi, v[e]);
+                    hn = fmax_nan(hn, v[e]);
+                }
             }
         }
 #pragma unroll
