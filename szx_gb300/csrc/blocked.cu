@@ -34,8 +34,13 @@
 
 namespace szxg {
 
-constexpr int kEncWarps = 8;
-constexpr int kEncThreads = kEncWarps * 32;
+// Encoder tiles: ~16 KiB of input per tile, as many warps as the tile has
+// block groups (at least 4), 24 warps per SM.  Measured on 512^3 fp32: 8 KiB
+// tiles in 4-warp CTAs (6 per SM) encode in 0.396 ms against 0.380 ms -- the
+// extra look-backs and tile claims cost more than the extra barrier domains
+// save.
+constexpr int kEncTileBytes = 16384;
+constexpr int kEncWarpsPerSm = 24;
 constexpr int kIdxThreads = 256;
 constexpr int kIdxItems = 8;   // items per thread in the index scans
 
@@ -240,49 +245,56 @@ struct EncTile {
     static constexpr int E = EncCfg<T>::E;
     static constexpr int kBsMax = G * E;                               // largest block of this variant
     static constexpr int kBpw = 32 / G;                                // blocks per warp
-    static constexpr int kRaw = 16384 / (kBsMax * (int)sizeof(T));
+    static constexpr int kRaw = kEncTileBytes / (kBsMax * (int)sizeof(T));
     static constexpr int kBlocks = kRaw >= 64 ? 64 : (kRaw < 8 ? 8 : kRaw);   // blocks per tile
+    static constexpr int kGroups = kBlocks / kBpw;                     // warps with blocks
+    static constexpr int kWarps = kGroups > 4 ? kGroups : 4;
+    static constexpr int kThreads = kWarps * 32;
+    static constexpr int kMinCtas = kEncWarpsPerSm / kWarps;
     static constexpr int kIn = kBlocks * kBsMax * (int)sizeof(T);      // input bytes per buffer
     static constexpr int kMaxPay = 5 + (kBsMax + 3) / 4 + (int)sizeof(T) * kBsMax;
     // payloads of a tile + slack for the word-wise reads of the realigning copy
     static constexpr int kStage = ((kBlocks * kMaxPay + 32 + 15) / 16) * 16;
-    static constexpr int kDynSmem = 2 * kIn + 2 * kStage;
-    static_assert(kBlocks / kBpw <= kEncWarps, "one block group per warp");
+    // a ring buffer holds a tile's input, then (in place) its payloads
+    static constexpr int kBuf = kIn > kStage ? kIn : kStage;
+    static constexpr int kDynSmem = 4 * kBuf;
+    static_assert(kGroups <= 8 && kBlocks % kBpw == 0, "one block group per warp");
     static_assert(kBlocks <= 64, "a tile's sizes are scanned as two warp-wide halves");
-    static_assert(kIn % 16 == 0 && kStage % 16 == 0, "TMA destinations stay 16-byte aligned");
+    static_assert(kIn % 16 == 0 && kBuf % 16 == 0, "TMA destinations stay 16-byte aligned");
 };
 
-// One pass over the input.  Per tile t_i (double-buffered input by TMA,
-// double-buffered staging), three CTA barriers:
-//   statistics of every block (registers)  |  barrier  |  refill of the input
-//   buffer with t_{i+2}; every warp scans the tile's block sizes for its own
-//   blocks' offsets (warp 0 publishes the tile's byte count) and emits them
-//   into staging, while warp 0 also places t_{i-1} by a look-back whose first
-//   loads were issued before its emission  |  barrier  |  copy-out of t_{i-1}
-//   to its place in the payload region  |  barrier.
-// Tile ids come from an atomic counter, taken in increasing order two tiles
-// ahead (the look-back stays deadlock-free with any number of resident CTAs);
-// the counter's reply is awaited only after the statistics.  A segment of G
-// lanes owns one block from its statistics to its emission; the look-back of a
-// tile runs one tile later than its publication, so predecessors have
-// normally published by then.
+// One pass over the input.  A CTA works through its tiles T_j in a ring of
+// four shared-memory buffers; iteration j, between two CTA barriers:
+//   TMA load of T_{j+1} (into the buffer T_{j-3} left); warp 0 places T_{j-2}
+//   from the look-back window copied in during iteration j-1; statistics of
+//   T_j's blocks (registers)  |  barrier  |  window copy for T_{j-1}; every
+//   warp scans T_j's block sizes for its own blocks' offsets (warp 0
+//   publishes T_j's byte count) and emits them into T_j's buffer in place
+//   (its input is dead); copy-out of T_{j-2} to its place in the payload
+//   region  |  barrier.
+// Every global round trip of a tile -- input load, tile claim, look-back --
+// thus has a whole iteration to complete.  Tile ids come from an atomic
+// counter, taken in increasing order two tiles ahead (the look-back stays
+// deadlock-free with any number of resident CTAs).  The look-back window
+// holds the 512 nearest predecessors, which normally reach back to this
+// CTA's own previous tile (already placed); otherwise it falls back to the
+// global walk.  A segment of G lanes owns one block from its statistics to
+// its emission.
 template <typename T, int G, bool MULTI>
-__global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
+__global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCtas) k_blocked_encode(EncArgs a) {
     using TL = EncTile<T, G>;
     constexpr int TB = TL::kBlocks;
     constexpr int BPW = TL::kBpw;
     constexpr int NGRP = TB / BPW;
     extern __shared__ __align__(128) uint8_t dsm[];
-    uint8_t* inb = dsm;
-    uint8_t* stgb = dsm + 2 * TL::kIn;
-    __shared__ unsigned long long bar[2];
-    __shared__ uint32_t s_size[2][TB], s_med[2][TB];
-    __shared__ uint8_t s_state[2][TB];
-    __shared__ uint32_t s_agg[2];
-    __shared__ long long s_tile[2];     // launch-wide tile index held by each input buffer
-    __shared__ int s_fld[2];            // its field
-    __shared__ long long s_next;        // the tile taken during the current one
-    __shared__ int s_fnext;
+    __shared__ unsigned long long bar[4];
+    __shared__ __align__(16) unsigned long long s_lbw[kLbWin];   // look-back window (status words)
+    __shared__ unsigned long long bar_lb;
+    __shared__ uint32_t s_size[4][TB], s_med[4][TB];
+    __shared__ uint8_t s_state[4][TB];
+    __shared__ uint32_t s_agg[4];
+    __shared__ long long s_tile[4];     // launch-wide tile index of each ring position
+    __shared__ int s_fld[4];            // its field
     __shared__ unsigned long long s_base;
     __shared__ int s_skip;
     const int warp = threadIdx.x >> 5;
@@ -293,19 +305,21 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     const bool vec = ((a.bs * (int)sizeof(T)) & 15) == 0;   // every block starts 16-byte aligned
     // field of a launch-wide tile: one load from the plan's tile map
     auto field_of = [&](long long g) { return (int)a.tile_field[g]; };
+    auto buf_ptr = [&](int r) { return dsm + r * TL::kBuf; };
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 2; i++) mbar_init(&bar[i], 1);
+        for (int r = 0; r < 4; r++) mbar_init(&bar[r], 1);
+        mbar_init(&bar_lb, 1);
         mbar_fence_init();
-        for (int i = 0; i < 2; i++) {
-            s_tile[i] = (long long)atomicAdd(a.tile_ctr, 1ull);
-            s_fld[i] = (MULTI && s_tile[i] < nt) ? field_of(s_tile[i]) : 0;
+        for (int r = 0; r < 2; r++) {
+            s_tile[r] = (long long)atomicAdd(a.tile_ctr, 1ull);
+            s_fld[r] = (MULTI && s_tile[r] < nt) ? field_of(s_tile[r]) : 0;
         }
     }
     __syncthreads();
     // a field's members: from the kernel parameters for one field, from the table for a batch
     auto fld = [&](int f) -> const BlkField* { return MULTI ? a.fields + f : nullptr; };
 #define FV(F_, m) (MULTI ? (F_)->m : a.one.m)
-    uint32_t phase = 0;   // bit i: parity to wait for on input buffer i
+    uint32_t phase = 0;   // bit r: parity to wait for on ring buffer r
 
     auto tile_count = [&](const BlkField* F, long long t) {
         const unsigned long long start = (unsigned long long)t * tile_elems;
@@ -313,7 +327,7 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         return rem < tile_elems ? rem : tile_elems;
     };
     // all threads: TMA of the 16-byte part by thread 0, the rest by plain copies
-    auto issue = [&](long long g, int f, int which) {
+    auto issue = [&](long long g, int f, int r) {
         const BlkField* F = fld(f);
         const long long t = g - (long long)FV(F, enc_tile0);
         const T* x = (const T*)FV(F, x);
@@ -321,19 +335,19 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         const unsigned long long cnt = tile_count(F, t);
         const uint32_t bytes = (uint32_t)(cnt * sizeof(T));
         const uint32_t tbytes = tma_ok ? (bytes & ~15u) : 0u;
-        T* dst = (T*)(inb + which * TL::kIn);
+        T* dst = (T*)buf_ptr(r);
         const T* src = x + (unsigned long long)t * tile_elems;
         if (threadIdx.x == 0 && tbytes) {
-            fence_proxy_async();
-            mbar_arrive_expect_tx(&bar[which], tbytes);
-            tma_load_1d(dst, src, tbytes, &bar[which]);
+            fence_proxy_async();   // the buffer's last generic accesses come before the async write
+            mbar_arrive_expect_tx(&bar[r], tbytes);
+            tma_load_1d(dst, src, tbytes, &bar[r]);
         }
-        for (unsigned long long i = tbytes / sizeof(T) + threadIdx.x; i < cnt; i += kEncThreads) dst[i] = src[i];
+        for (unsigned long long i = tbytes / sizeof(T) + threadIdx.x; i < cnt; i += TL::kThreads) dst[i] = src[i];
     };
-    auto wait_buf = [&](const BlkField* F, long long t, int which) {
+    auto wait_buf = [&](const BlkField* F, long long t, int r) {
         if (((uintptr_t)FV(F, x) & 15) == 0 && ((tile_count(F, t) * sizeof(T)) & ~15ull)) {
-            if (!mbar_wait(&bar[which], (phase >> which) & 1u) && threadIdx.x == 0) atomicExch(a.err, kErrLookback);
-            phase ^= 1u << which;
+            if (!mbar_wait(&bar[r], (phase >> r) & 1u) && threadIdx.x == 0) atomicExch(a.err, kErrLookback);
+            phase ^= 1u << r;
         }
     };
     auto block_len = [&](const BlkField* F, long long t, int lb) {
@@ -344,10 +358,30 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
     };
 
     unsigned long long nnc_cta = 0;   // warp 0 lane 0, single field: non-constant blocks of this CTA's tiles
-    // warp 0: offset of tile t of field F (slot), its sizes / medians / state bits by block
-    auto resolve = [&](const BlkField* F, long long t, int slot, const LookbackWin& lw) {
-        const uint32_t agg = s_agg[slot];
-        const unsigned long long base = prefix_resolve_pre(FV(F, st_enc), t, agg, a.err, lw);
+    // thread 0: copy the status words of tile t's predecessors [lo, t) (at most
+    // kLbWin, the nearest ones) to shared memory; returns lo
+    uint32_t lb_phase = 0;
+    auto window_load = [&](const BlkField* F, long long t) -> long long {
+        if (t <= 0) return 0;
+        long long lo = t > kLbWin ? t - kLbWin : 0;
+        lo = (lo + 1) & ~1ll;                                           // 16-byte aligned source
+        const uint32_t bytes = (uint32_t)(((t - lo + 1) & ~1ll) * 8);   // whole 16-byte units, within st
+        if (threadIdx.x == 0) {
+            fence_proxy_async();   // the window's last reads and this CTA's publications come first
+            mbar_arrive_expect_tx(&bar_lb, bytes);
+            tma_load_1d(s_lbw, FV(F, st_enc) + lo, bytes, &bar_lb);
+        }
+        return lo;
+    };
+    // warp 0: offset of tile t of field F (metadata set r), its sizes / medians / state bits by block
+    auto resolve = [&](const BlkField* F, long long t, int r, long long lo) {
+        const uint32_t agg = s_agg[r];
+        unsigned long long base = 0;
+        if (t > 0) {
+            if (!mbar_wait(&bar_lb, lb_phase) && lane == 0) atomicExch(a.err, kErrLookback);
+            lb_phase ^= 1u;
+            base = prefix_resolve_win(FV(F, st_enc), t, agg, a.err, s_lbw, lo);
+        }
         const bool cap_ok = base + agg <= FV(F, payload_cap);
         const unsigned long long tb0 = (unsigned long long)t * TB;
         uint32_t m01[2];
@@ -355,10 +389,10 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         for (int h = 0; h < 2; h++) {
             const int lb = lane + 32 * h;
             const bool in = lb < TB;
-            const int st = in ? s_state[slot][lb] : 2;
+            const int st = in ? s_state[r][lb] : 2;
             if (in && st != 2) {
-                FV(F, size_blk)[tb0 + lb] = (uint16_t)s_size[slot][lb];
-                FV(F, med_blk)[tb0 + lb] = s_med[slot][lb];
+                FV(F, size_blk)[tb0 + lb] = (uint16_t)s_size[r][lb];
+                FV(F, med_blk)[tb0 + lb] = s_med[r][lb];
             }
             m01[h] = __ballot_sync(0xffffffffu, in && st == 1);
         }
@@ -377,28 +411,34 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
             s_skip = !cap_ok;
         }
     };
+    auto copy_out = [&](const BlkField* F, int r) {
+        if (!s_skip) cta_copy_realign(buf_ptr(r), s_agg[r], FV(F, payload) + s_base);
+    };
 
-    {
-        const long long g0 = s_tile[0], g1 = s_tile[1];
-        if (g0 < nt) issue(g0, s_fld[0], 0);
-        if (g1 < nt) issue(g1, s_fld[1], 1);
-    }
-    const bool taker = warp == kEncWarps - 1 && lane == 0;
-    long long t_prev = -1;
-    int f_prev = 0;
-    int i = 0;
-    for (;; i++) {
-        const int slot = i & 1;
-        __syncthreads();   // s_tile of this slot, previous copy-out done
-        const long long g = s_tile[slot];
+    if (s_tile[0] < nt) issue(s_tile[0], s_fld[0], 0);
+    const bool taker = warp == TL::kWarps - 1 && lane == 0;
+    long long t1 = -1, t2 = -1;   // T_{j-1}, T_{j-2} (field-local), -1: none
+    int f1 = 0, f2 = 0;
+    long long lo1 = 0;            // window base of T_{j-1}
+    int j = 0;
+    for (;; j++) {
+        const int r = j & 3;
+        __syncthreads();   // ring position j+1 claimed, copy-out of T_{j-3} done
+        {
+            const int rn = (j + 1) & 3;
+            const long long gn = s_tile[rn];
+            if (gn < nt) issue(gn, s_fld[rn], rn);
+        }
+        if (warp == 0 && t2 >= 0) resolve(fld(f2), t2, (j - 2) & 3, lo1);
+        const long long g = s_tile[r];
         if (g >= nt) break;
-        const int f = s_fld[slot];
+        const int f = s_fld[r];
         const BlkField* F = fld(f);
         const long long t = g - (long long)FV(F, enc_tile0);
-        // the last warp takes this buffer's next tile; the reply is used after the statistics
-        unsigned long long gn = 0;
-        if (taker) gn = atomicAdd(a.tile_ctr, 1ull);
-        wait_buf(F, t, slot);
+        // the last warp takes the tile of ring position j+2; the reply is used after the statistics
+        unsigned long long gc = 0;
+        if (taker) gc = atomicAdd(a.tile_ctr, 1ull);
+        wait_buf(F, t, r);
         // ---- statistics of the tile's blocks, one block per segment
         const int lb = warp * BPW + seg;
         const bool mine = warp < NGRP;
@@ -407,35 +447,26 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         BlockEnc<T> b;
         if (mine) {
             const float eb = FV(F, params) ? FV(F, params)->eb : FV(F, eb);
-            const T* xs = (const T*)(inb + slot * TL::kIn) + (size_t)lb * a.bs;
+            const T* xs = (const T*)buf_ptr(r) + (size_t)lb * a.bs;
             if (full) enc_block_stats<T, G, true>(xs, len, vec, eb, a.omp_stats, b);
             else enc_block_stats<T, G, false>(xs, len, vec, eb, a.omp_stats, b);
             if (sl == 0) {
-                s_state[slot][lb] = (uint8_t)b.state;
-                s_size[slot][lb] = b.state == 1 ? b.size : 0;
-                s_med[slot][lb] = b.med_bits;
+                s_state[r][lb] = (uint8_t)b.state;
+                s_size[r][lb] = b.state == 1 ? b.size : 0;
+                s_med[r][lb] = b.med_bits;
             }
         }
         if (taker) {
-            s_next = (long long)gn;
-            s_fnext = (MULTI && (long long)gn < nt) ? field_of((long long)gn) : 0;
+            const int rc = (j + 2) & 3;   // T_{j-2}'s position: its id was read two barriers ago
+            s_tile[rc] = (long long)gc;
+            s_fld[rc] = (MULTI && (long long)gc < nt) ? field_of((long long)gc) : 0;
         }
-        __syncthreads();   // statistics in, input buffer free, next tile id known
-        {
-            const long long gq = s_next;
-            const int fq = s_fnext;
-            if (gq < nt) issue(gq, fq, slot);
-            if (threadIdx.x == 0) {   // read again two tiles on, after the barriers between
-                s_tile[slot] = gq;
-                s_fld[slot] = fq;
-            }
-        }
-        // warp 0: the previous tile's first look-back window, in flight during the emission
-        LookbackWin lw;
-        if (warp == 0 && t_prev >= 0) lookback_load(FV(fld(f_prev), st_enc), t_prev, lw);
+        __syncthreads();   // statistics in (T_j's input is dead), T_{j-2} placed
+        // warp 0: T_{j-1}'s look-back window, in flight until the next iteration
+        if (warp == 0 && t1 >= 0) lo1 = window_load(fld(f1), t1);
         // every warp: the tile's block offsets (two warp-wide halves)
         const bool in0 = lane < TB, in1 = lane + 32 < TB;
-        const uint32_t sz0 = in0 ? s_size[slot][lane] : 0, sz1 = in1 ? s_size[slot][lane + 32] : 0;
+        const uint32_t sz0 = in0 ? s_size[r][lane] : 0, sz1 = in1 ? s_size[r][lane + 32] : 0;
         const uint32_t i0 = warp_inclusive_sum(sz0);
         const uint32_t c0 = __shfl_sync(0xffffffffu, i0, 31);
         const uint32_t i1 = warp_inclusive_sum(sz1) + c0;
@@ -444,32 +475,34 @@ __global__ void __launch_bounds__(kEncThreads, 3) k_blocked_encode(EncArgs a) {
         const uint32_t loc_hi = __shfl_sync(0xffffffffu, e1, lb & 31);
         if (warp == 0) {
             const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
-            if (lane == 0) s_agg[slot] = agg;
+            if (lane == 0) s_agg[r] = agg;
             prefix_publish(FV(F, st_enc), t, agg);
         }
         if (mine && b.state == 1) {
-            uint8_t* stg = stgb + slot * TL::kStage;
             const uint32_t loc = lb < 32 ? loc_lo : loc_hi;
-            if (full) enc_block_emit<T, G, true>(stg, loc, len, b);
-            else enc_block_emit<T, G, false>(stg, loc, len, b);
+            if (full) enc_block_emit<T, G, true>(buf_ptr(r), loc, len, b);
+            else enc_block_emit<T, G, false>(buf_ptr(r), loc, len, b);
         }
-        if (warp == 0 && t_prev >= 0) resolve(fld(f_prev), t_prev, slot ^ 1, lw);
-        __syncthreads();   // payloads staged, previous tile placed
-        if (t_prev >= 0 && !s_skip)
-            cta_copy_realign(stgb + (slot ^ 1) * TL::kStage, s_agg[slot ^ 1], FV(fld(f_prev), payload) + s_base);
-        t_prev = t;
-        f_prev = f;
+        if (t2 >= 0) copy_out(fld(f2), (j - 2) & 3);
+        t2 = t1;
+        f2 = f1;
+        t1 = t;
+        f1 = f;
     }
-    // the last tile of this CTA: placed and written out after the loop
-    if (t_prev >= 0) {
-        const int ps = (i & 1) ^ 1;
+    // this CTA's last two tiles: T_{j-2} was placed at the top of the final
+    // iteration, T_{j-1} still needs its look-back
+    if (t2 >= 0) {
+        __syncthreads();
+        copy_out(fld(f2), (j - 2) & 3);
+    }
+    if (t1 >= 0) {
+        __syncthreads();   // the window buffer and s_base are free again
         if (warp == 0) {
-            LookbackWin lw;
-            lookback_load(FV(fld(f_prev), st_enc), t_prev, lw);
-            resolve(fld(f_prev), t_prev, ps, lw);
+            const long long lo = window_load(fld(f1), t1);
+            resolve(fld(f1), t1, (j - 1) & 3, lo);
         }
         __syncthreads();
-        if (!s_skip) cta_copy_realign(stgb + ps * TL::kStage, s_agg[ps], FV(fld(f_prev), payload) + s_base);
+        copy_out(fld(f1), (j - 1) & 3);
     }
     if (threadIdx.x == 0 && nnc_cta) atomicAdd(&a.one.tot->nnc, nnc_cta);
 #undef FV
@@ -659,7 +692,7 @@ static cudaError_t run_encode(EncArgs a, cudaStream_t s) {
         }
         int occ = 0;
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_blocked_encode<T, G, false>, kEncThreads,
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_blocked_encode<T, G, false>, TL::kThreads,
                                                               TL::kDynSmem);
         if (e != cudaSuccess) return e;
         per_sm[dev] = occ < 1 ? 1 : occ;
@@ -668,8 +701,8 @@ static cudaError_t run_encode(EncArgs a, cudaStream_t s) {
     const size_t g = (size_t)sm_count() * per_sm[dev];
     const int grid = (int)(a.total_tiles < g ? a.total_tiles : g);
     TraceScope tr("blocked_encode", s);
-    if (a.nf > 1) k_blocked_encode<T, G, true><<<grid, kEncThreads, TL::kDynSmem, s>>>(a);
-    else k_blocked_encode<T, G, false><<<grid, kEncThreads, TL::kDynSmem, s>>>(a);
+    if (a.nf > 1) k_blocked_encode<T, G, true><<<grid, TL::kThreads, TL::kDynSmem, s>>>(a);
+    else k_blocked_encode<T, G, false><<<grid, TL::kThreads, TL::kDynSmem, s>>>(a);
     return cudaGetLastError();
 }
 
