@@ -677,33 +677,44 @@ __device__ __forceinline__ unsigned long long prefix_resolve_pre(unsigned long l
 
 // The look-back from a window of status words that a TMA bulk copy has put
 // in shared memory: win[i] holds the word of tile lo + i, for every tile in
-// [lo, tile).  The warp walks it in rows of 32 consecutive tiles, newest
-// first (one word per lane, conflict-free), and stops at the nearest
-// inclusive prefix.  A window that holds no inclusive prefix, or an empty
-// word before it, falls back to the global look-back (which then waits);
-// either way the tile's inclusive value is published and its exclusive
-// prefix returned.
+// [lo, tile).  Lane l reads the words of tiles tile-1-l-32k (k = 0..15, rows
+// of 32 consecutive tiles, conflict-free) all at once; the nearest inclusive
+// prefix is the lowest (row, lane) holding one, found with two warp
+// reductions, so the walk is a handful of independent instructions rather
+// than a chain of dependent rows.  A window that holds no inclusive prefix,
+// or an empty word before it, falls back to the global look-back (which then
+// waits); either way the tile's inclusive value is published and its
+// exclusive prefix returned.
 constexpr int kLbWin = 512;   // status words per window (4 KiB)
 __device__ __forceinline__ unsigned long long prefix_resolve_win(unsigned long long* st, long long tile,
                                                                 unsigned long long agg, int* err,
                                                                 const unsigned long long* win, long long lo) {
     if (tile == 0) return 0;
+    constexpr int R = kLbWin / 32;
     const unsigned lane = lane_id();
-    unsigned long long sa = 0;
-    bool ok = false;
-#pragma unroll 1
-    for (int k = 0; k < kLbWin / 32; k++) {
+    unsigned long long w[R];
+    unsigned first = R;   // this lane's first row holding an inclusive word
+#pragma unroll
+    for (int k = 0; k < R; k++) {
         const long long j = tile - 1 - 32 * (long long)k - (long long)lane;
-        const bool in = j >= lo;
-        const unsigned long long w = in ? win[j - lo] : 0ull;
-        const unsigned long long f = w & ~kS64Val;
-        const unsigned incm = __ballot_sync(0xffffffffu, in && f == kS64Inc);
-        const unsigned stop = incm ? (unsigned)__ffs(incm) - 1 : 32u;
-        const bool take = in && lane <= stop;
-        if (__ballot_sync(0xffffffffu, take && f == 0)) break;   // an unpublished predecessor
-        if (take) sa += w & kS64Val;
-        if (incm) { ok = true; break; }
-        if (!__any_sync(0xffffffffu, in)) break;                  // the window is exhausted
+        w[k] = j >= lo ? win[j - lo] : 0ull;   // outside the window reads as empty
+        if (first == R && (w[k] & ~kS64Val) == kS64Inc) first = k;
+    }
+    const unsigned K = __reduce_min_sync(0xffffffffu, first);
+    bool ok = K < R;
+    unsigned long long sa = 0;
+    if (ok) {
+        const unsigned stop = __ffs(__ballot_sync(0xffffffffu, first == K)) - 1;
+        bool ready = true;
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            const bool take = (unsigned)k < K || ((unsigned)k == K && lane <= stop);
+            if (take) {
+                ready = ready && (w[k] & ~kS64Val) != 0;
+                sa += w[k] & kS64Val;
+            }
+        }
+        ok = __all_sync(0xffffffffu, ready);
     }
     if (!ok) return prefix_resolve(st, tile, agg, err);
     const unsigned long long pa = warp_sum(sa);
