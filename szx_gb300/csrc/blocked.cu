@@ -1168,6 +1168,8 @@ __device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bo
 constexpr int kDecWarps = 8;
 constexpr int kDecThreadsP = (kDecWarps + 1) * 32;
 constexpr int kDecStages = 3;
+// 4 CTAs of 9 warps per SM (56 registers, three ring stages of shared memory)
+constexpr int kDecCtasPerSm = 4;
 
 template <typename T, int G>
 struct DecTileV {
@@ -1200,7 +1202,7 @@ struct DecArgs {
 enum : uint8_t { kBlkConst = 0, kBlkCoded = 1, kBlkNone = 2 };
 
 template <typename T, int G, bool MULTI>
-__global__ void __launch_bounds__(kDecThreadsP, 3) k_blocked_decode(DecArgs a) {
+__global__ void __launch_bounds__(kDecThreadsP, kDecCtasPerSm) k_blocked_decode(DecArgs a) {
     using TL = DecTileV<T, G>;
     constexpr int TB = TL::kBlocks;
     constexpr int NS = kDecStages;
@@ -1438,7 +1440,7 @@ static cudaError_t run_decode(const uint8_t* s, size_t len, size_t nb, const Wor
     cudaError_t e = dec_attr<T, G, false>();
     if (e != cudaSuccess) return e;
     const size_t tiles = (nb + TL::kBlocks - 1) / TL::kBlocks;
-    const size_t cap = (size_t)sm_count() * 3;
+    const size_t cap = (size_t)sm_count() * kDecCtasPerSm;
     const int grid = (int)(tiles < cap ? (tiles ? tiles : 1) : cap);
     DecArgs a = {};
     a.s = s; a.len = len; a.hdr = ws.bhdr; a.P = ws.p_off; a.RW = ws.rank_w; a.out = out;
@@ -1454,7 +1456,7 @@ static cudaError_t run_decode_fields(const DecField* F, const uint32_t* tf, int 
     using TL = DecTileV<T, G>;
     cudaError_t e = dec_attr<T, G, true>();
     if (e != cudaSuccess) return e;
-    const size_t cap = (size_t)sm_count() * 3;
+    const size_t cap = (size_t)sm_count() * kDecCtasPerSm;
     const int grid = (int)(total < cap ? (total ? total : 1) : cap);
     DecArgs a = {};
     a.native_medians = native; a.err = lerr;
