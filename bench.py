@@ -185,6 +185,22 @@ def run_reference(args, wl, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def reduce_over_ranks(maxes, sums, device):
+    """The replicas' only cross-rank step (timing, never data): each value of
+    `maxes` becomes its maximum over the ranks (a job ends with its slowest
+    rank) and each value of `sums` its sum.  Needs an initialised
+    torch.distributed process group (NCCL on GPUs; gloo in the CPU tests)."""
+    import torch
+    import torch.distributed as D
+    m = torch.tensor([float(v) for v in maxes], dtype=torch.float64, device=device)
+    s = torch.tensor([float(v) for v in sums], dtype=torch.float64, device=device)
+    if m.numel():
+        D.all_reduce(m, op=D.ReduceOp.MAX)
+    if s.numel():
+        D.all_reduce(s, op=D.ReduceOp.SUM)
+    return m.tolist(), s.tolist()
+
+
 def run_ours(args, wl, rank, world, local_rank):
     import numpy as np
     import torch
@@ -258,12 +274,8 @@ def run_ours(args, wl, rank, world, local_rank):
     bound_ok = bool((err <= eb + 2 * ulp.double()).all().item())
 
     if dist:
-        t = torch.tensor([total_ms, tc, td, launches], dtype=torch.float64, device="cuda")
-        tmax = t.clone()
-        D.all_reduce(tmax[:3], op=D.ReduceOp.MAX)
-        D.all_reduce(t[3:], op=D.ReduceOp.SUM)
-        total_ms, tc, td = tmax[0].item(), tmax[1].item(), tmax[2].item()
-        launches = int(t[3].item())
+        (total_ms, tc, td), (launches,) = reduce_over_ranks([total_ms, tc, td], [launches], "cuda")
+        launches = int(launches)
 
     # ---- e2e through the reference-facing entry points, host buffers
     xh = torch.empty(n, dtype=torch.float32, pin_memory=True)
@@ -293,9 +305,7 @@ def run_ours(args, wl, rank, world, local_rank):
         e2e_step()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     if dist:
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        D.all_reduce(tt, op=D.ReduceOp.MAX)
-        e2e_s = tt.item()
+        (e2e_s,), _ = reduce_over_ranks([e2e_s], [], "cuda")
 
     if rank != 0:
         return
