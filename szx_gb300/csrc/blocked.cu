@@ -97,13 +97,13 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
     float radius_f, median_f;
     if constexpr (sizeof(T) == 4) {
         const float range = xsub(mx, mn);
-        radius_f = xdiv(range, 2.0f);
+        radius_f = xhalf(range);
         median_f = xadd(mn, radius_f);
         state = (radius_f <= eb) ? 0 : 1;
     } else if (!omp_stats) {
         // szx/src/szx_double.cc:991-1003: double statistics, float median/radius
         const double range = xsub(mx, mn);
-        const double radius = xdiv(range, 2.0);
+        const double radius = xhalf(range);
         const double median = xadd(mn, radius);
         state = (radius <= (double)eb) ? 0 : 1;
         radius_f = xd2f(radius);
@@ -111,7 +111,7 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
     } else {
         // computeStateMedianRadius_double2 (szx/src/szx_double.cc:1120-1135)
         const double range = xsub(mx, mn);
-        radius_f = xd2f(xdiv(range, 2.0));
+        radius_f = xd2f(xhalf(range));
         median_f = xd2f(xadd(mn, xf2d(radius_f)));
         state = (radius_f <= eb) ? 0 : 1;
     }

@@ -70,6 +70,12 @@ __device__ __forceinline__ double xsub(double a, double b) { double r = __dsub_r
 __device__ __forceinline__ double xadd(double a, double b) { double r = __dadd_rn(a, b); return r == r ? r : nan_rule(a, b); }
 __device__ __forceinline__ double xmul(double a, double b) { double r = __dmul_rn(a, b); return r == r ? r : nan_rule(a, b); }
 __device__ __forceinline__ double xdiv(double a, double b) { double r = __ddiv_rn(a, b); return r == r ? r : nan_rule(a, b); }
+// x / 2 as a multiplication: both are the correctly rounded value of the same
+// real number (subnormal results included), and a NaN x propagates the same
+// way, so the result is bit-identical to the division at a fraction of its
+// cost.
+__device__ __forceinline__ float xhalf(float x) { return xmul(x, 0.5f); }
+__device__ __forceinline__ double xhalf(double x) { return xmul(x, 0.5); }
 // cvtsd2ss / cvtss2sd
 __device__ __forceinline__ float xd2f(double d) {
     if (d == d) return __double2float_rn(d);

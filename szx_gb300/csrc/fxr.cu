@@ -92,11 +92,11 @@ __global__ void __launch_bounds__(kFxThreads) k_fxr_sample(const T* x, unsigned 
     (void)special;
     if (in && sl == 0) {
         if constexpr (sizeof(T) == 4) {
-            const float r = xdiv(xsub(mx, mn), 2.0f);
+            const float r = xhalf(xsub(mx, mn));
             rads[i] = r;
             meds[i] = xadd(mn, r);
         } else {
-            const double r = xdiv(xsub(mx, mn), 2.0);
+            const double r = xhalf(xsub(mx, mn));
             rads[i] = xd2f(r);
             meds[i] = xd2f(xadd(mn, r));
             rads_d[i] = r;
