@@ -48,16 +48,28 @@ constexpr int kIdxItems = 8;   // items per thread in the index scans
 //
 // Per-block state a segment keeps in registers from its statistics pass to
 // its emission (szx/src/szx_float.cc:49-252 for one block).
-template <typename T>
+// Chunk-round byte totals of a segment are scanned packed, one field per
+// round: 8-bit fields for float up to 8 lanes (a round holds at most 8 x 16
+// bytes), 16-bit otherwise; in 32 bits whenever they fit.
+template <typename T, int G>
+struct RoundPack {
+    static constexpr int NC = EncCfg<T>::E / 4;
+    static constexpr int FB = (sizeof(T) == 4 && G <= 8) ? 8 : 16;
+    static constexpr uint32_t MASK = (1u << FB) - 1;
+    using P = typename std::conditional<NC * FB <= 32, uint32_t, unsigned long long>::type;
+};
+
+template <typename T, int G>
 struct BlockEnc {
     using U = typename Elem<T>::U;
+    using P = typename RoundPack<T, G>::P;
     static constexpr int E = EncCfg<T>::E;
     static constexpr int NC = E / 4;
     U cur[E];                        // shifted words
     uint32_t cnt4[NC];               // stored bytes of the chunk's 4 values (byte i: value i)
     uint32_t pre4[NC];               // exclusive offsets of those bytes within the chunk
     uint32_t codes;                  // lead byte of chunk round k in byte k
-    unsigned long long excl, tot;    // per round (16-bit fields): bytes of earlier lanes, round total
+    P excl, tot;                     // per round (packed fields): bytes of earlier lanes, round total
     int state;                       // 0 constant, 1 coded, 2 no block
     int reqLength;
     uint32_t med_bits;               // median as stored (payload or constant list)
@@ -80,9 +92,11 @@ struct EncArgs {
 // median (szx/src/szx_float.cc:314-371), the shifted words, lead codes
 // (szx/src/szx_float.cc:94-113) and stored-byte counts, all kept in registers.
 template <typename T, int G, bool FULL>
-__device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, float eb, int omp_stats,
-                                                BlockEnc<T>& b) {
+__device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, float eb, int eb_exp, int omp_stats,
+                                                BlockEnc<T, G>& b) {
     using C = Chunks<T, G>;
+    using RP = RoundPack<T, G>;
+    using P = typename RP::P;
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int E = C::E;
@@ -116,7 +130,7 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
         state = (radius_f <= eb) ? 0 : 1;
     }
     bool zm;
-    const int reqLength = req_length<T>(eb, radius_f, &zm);
+    const int reqLength = req_length_e<T>(eb_exp, radius_f, &zm);
     int R, s;
     split_reqlen(reqLength, &R, &s);
     const uint32_t payload_med = zm ? 0u : __float_as_uint(median_f);
@@ -135,7 +149,7 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
     uint32_t ldbs[NC];
     seg_lead_bytes<T, G>(b.cur, ldbs);
     const uint32_t R4 = (uint32_t)R * 0x01010101u;
-    unsigned long long pk = 0;
+    P pk = 0;
     uint32_t codes = 0;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
@@ -148,16 +162,16 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
         }
         b.cnt4[k] = cnt4;
         b.pre4[k] = cnt4 * 0x01010100u;
-        pk |= (unsigned long long)((cnt4 * 0x01010101u) >> 24) << (16 * k);
+        pk |= (P)((cnt4 * 0x01010101u) >> 24) << (RP::FB * k);
         codes |= ((ldb * 0x40100401u) >> 24) << (8 * k);   // 4 leads -> one byte, MSB first
     }
-    const unsigned long long incl = seg_inclusive_sum<G>(pk);
+    const P incl = seg_inclusive_sum<G>(pk);
     b.tot = __shfl_sync(0xffffffffu, incl, G - 1, G);
     b.excl = incl - pk;
     b.codes = codes;
     uint32_t mid = 0;
 #pragma unroll
-    for (int k = 0; k < NC; k++) mid += (uint32_t)((b.tot >> (16 * k)) & 0xFFFF);
+    for (int k = 0; k < NC; k++) mid += (uint32_t)((b.tot >> (RP::FB * k)) & RP::MASK);
     const int Lb = FULL ? G * NC : (len + 3) / 4;
     b.size = 5 + (uint32_t)Lb + mid;
     b.state = len ? state : 2;
@@ -171,7 +185,8 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
 // needs no clearing and no atomics (a value's bytes are contiguous, values
 // follow each other without gaps).
 template <typename T, int G, bool FULL>
-__device__ __forceinline__ void enc_block_emit(uint8_t* stg, uint32_t loc, int len, const BlockEnc<T>& b) {
+__device__ __forceinline__ void enc_block_emit(uint8_t* stg, uint32_t loc, int len, const BlockEnc<T, G>& b) {
+    using RP = RoundPack<T, G>;
     using C = Chunks<T, G>;
     using EL = Elem<T>;
     using U = typename EL::U;
@@ -197,8 +212,8 @@ __device__ __forceinline__ void enc_block_emit(uint8_t* stg, uint32_t loc, int l
         const int c = sl + k * G;
         // lead codes: 4 per byte, MSB first (szx/src/szx_TypeManager.cc:198-273)
         if (FULL || c < Lb) p[5 + c] = (uint8_t)(b.codes >> (8 * k));
-        const uint32_t qb = before + (uint32_t)((b.excl >> (16 * k)) & 0xFFFF);
-        before += (uint32_t)((b.tot >> (16 * k)) & 0xFFFF);
+        const uint32_t qb = before + (uint32_t)((b.excl >> (RP::FB * k)) & RP::MASK);
+        before += (uint32_t)((b.tot >> (RP::FB * k)) & RP::MASK);
         // mid bytes: bytes [W-R .. W-1-lead] of each shifted word, ascending
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -418,6 +433,8 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
     if (s_tile[0] < nt) issue(s_tile[0], s_fld[0], 0);
     const bool taker = warp == TL::kWarps - 1 && lane == 0;
     long long t1 = -1, t2 = -1;   // T_{j-1}, T_{j-2} (field-local), -1: none
+    int eb_f = -1, eb_exp = 0;    // field whose bound is loaded, the bound's exponent
+    float eb = 0.f;
     int f1 = 0, f2 = 0;
     long long lo1 = 0;            // window base of T_{j-1}
     int j = 0;
@@ -444,12 +461,16 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
         const bool mine = warp < NGRP;
         const int len = mine ? block_len(F, t, lb) : 0;
         const bool full = __all_sync(0xffffffffu, len == TL::kBsMax);
-        BlockEnc<T> b;
+        if (f != eb_f) {   // the field's bound and its exponent, once per field
+            eb = FV(F, params) ? FV(F, params)->eb : FV(F, eb);
+            eb_exp = exponent_f64_of_f32(eb);
+            eb_f = f;
+        }
+        BlockEnc<T, G> b;
         if (mine) {
-            const float eb = FV(F, params) ? FV(F, params)->eb : FV(F, eb);
             const T* xs = (const T*)buf_ptr(r) + (size_t)lb * a.bs;
-            if (full) enc_block_stats<T, G, true>(xs, len, vec, eb, a.omp_stats, b);
-            else enc_block_stats<T, G, false>(xs, len, vec, eb, a.omp_stats, b);
+            if (full) enc_block_stats<T, G, true>(xs, len, vec, eb, eb_exp, a.omp_stats, b);
+            else enc_block_stats<T, G, false>(xs, len, vec, eb, eb_exp, a.omp_stats, b);
             if (sl == 0) {
                 s_state[r][lb] = (uint8_t)b.state;
                 s_size[r][lb] = b.state == 1 ? b.size : 0;

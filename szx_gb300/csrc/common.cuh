@@ -101,20 +101,26 @@ __device__ __forceinline__ int exponent_f64_of_f32(float v) {
 // computeReqLength_float (szx/src/szx_float.cc:1708-1717) / _double
 // (szx/src/szx_double.cc:2020-2031).  Returns reqLength; *zero_median set when
 // the clamp at the word width zeroes the stored median.
-template <typename T> __device__ __forceinline__ int req_length(float eb, float radius, bool* zero_median);
-template <> __device__ __forceinline__ int req_length<float>(float eb, float radius, bool* zm) {
-    int r = 10 + exponent_f32(radius) - exponent_f64_of_f32(eb);
+// The bound's exponent (exponent_f64_of_f32(eb)) is a per-field constant:
+// callers that place many blocks under one bound compute it once and use the
+// eb_exp overloads.
+template <typename T> __device__ __forceinline__ int req_length_e(int eb_exp, float radius, bool* zero_median);
+template <> __device__ __forceinline__ int req_length_e<float>(int eb_exp, float radius, bool* zm) {
+    int r = 10 + exponent_f32(radius) - eb_exp;
     *zm = false;
     if (r < 9) r = 9;
     if (r > 32) { r = 32; *zm = true; }
     return r;
 }
-template <> __device__ __forceinline__ int req_length<double>(float eb, float radius, bool* zm) {
-    int r = 12 + exponent_f32(radius) - exponent_f64_of_f32(eb);
+template <> __device__ __forceinline__ int req_length_e<double>(int eb_exp, float radius, bool* zm) {
+    int r = 12 + exponent_f32(radius) - eb_exp;
     *zm = false;
     if (r < 12) r = 12;
     if (r > 64) { r = 64; *zm = true; }
     return r;
+}
+template <typename T> __device__ __forceinline__ int req_length(float eb, float radius, bool* zero_median) {
+    return req_length_e<T>(exponent_f64_of_f32(eb), radius, zero_median);
 }
 __device__ __forceinline__ void split_reqlen(int reqLength, int* R, int* s) {
     int rb = reqLength & 7;

@@ -149,11 +149,13 @@ __device__ __forceinline__ void seg_minmax(const T (&v)[EncCfg<T>::E], int len, 
         for (int d = G / 2; d > 0; d >>= 1) {
             lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, d, G));
             hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, d, G));
-            hn = fmax_nan(hn, __shfl_xor_sync(0xffffffffu, hn, d, G));
         }
         mn = lo;
         mx = hi;
-        special = isnan(hn) || isinf(lo) || isinf(hi);
+        // a NaN anywhere in the segment: one vote instead of a reduction
+        const unsigned seg0 = lane_id() & ~(unsigned)(G - 1);
+        const unsigned segmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << seg0);
+        special = (__ballot_sync(0xffffffffu, isnan(hn)) & segmask) != 0 || isinf(lo) || isinf(hi);
     } else {
         long long lo = 0x7FFFFFFFFFFFFFFFll, hi = (long long)0x8000000000000000ull;
         bool nan = false;
