@@ -148,13 +148,12 @@ __device__ __forceinline__ void enc_block_stats(const T* xs, int len, bool vec, 
     // lead codes: leading identical bytes with the previous value, capped at 3
     uint32_t ldbs[NC];
     seg_lead_bytes<T, G>(b.cur, ldbs);
-    const uint32_t R4 = (uint32_t)R * 0x01010101u;
     P pk = 0;
     uint32_t codes = 0;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
         uint32_t ldb = ldbs[k];
-        uint32_t cnt4 = __vsubus4(R4, ldb);   // max(R - lead, 0) per value
+        uint32_t cnt4 = stored_counts(R, ldb);   // max(R - lead, 0) per value
         if constexpr (!FULL) {
             const uint32_t m = low_bytes_mask(len - 4 * (sl + k * G));
             ldb &= m;
@@ -459,7 +458,9 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
         // ---- statistics of the tile's blocks, one block per segment
         const int lb = warp * BPW + seg;
         const bool mine = warp < NGRP;
-        const int len = mine ? block_len(F, t, lb) : 0;
+        // every tile but a field's last holds whole blocks only
+        const bool whole = (unsigned long long)(t + 1) * tile_elems <= FV(F, n);
+        const int len = !mine ? 0 : (whole ? a.bs : block_len(F, t, lb));
         const bool full = __all_sync(0xffffffffu, len == TL::kBsMax);
         if (f != eb_f) {   // the field's bound and its exponent, once per field
             eb = FV(F, params) ? FV(F, params)->eb : FV(F, eb);
@@ -1083,14 +1084,13 @@ __device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bo
     // per chunk: leads, running minima, stored-byte counts and their offsets (bytes of a word)
     uint32_t ldb[NC], cmb[NC], pre[NC];
     unsigned long long pk = 0;
-    const uint32_t R4 = (uint32_t)R * 0x01010101u;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
         const int c = sl + k * G;
         const uint32_t code = (FULL || c < Lb) ? (uint32_t)p[5 + c] : 0u;
         ldb[k] = lut_ld[code];
         cmb[k] = lut_cm[code];
-        uint32_t cnt4 = __vsubus4(R4, ldb[k]);   // max(R - lead, 0) per value
+        uint32_t cnt4 = stored_counts(R, ldb[k]);   // max(R - lead, 0) per value
         if constexpr (!FULL) {
             const int nin = len - 4 * c;
             cnt4 &= nin >= 4 ? 0xFFFFFFFFu : (nin <= 0 ? 0u : 0xFFFFFFFFu >> (32 - 8 * nin));

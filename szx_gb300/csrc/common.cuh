@@ -122,6 +122,18 @@ template <> __device__ __forceinline__ int req_length_e<double>(int eb_exp, floa
 template <typename T> __device__ __forceinline__ int req_length(float eb, float radius, bool* zero_median) {
     return req_length_e<T>(exponent_f64_of_f32(eb), radius, zero_median);
 }
+// Stored-byte counts of four values, max(R - lead, 0) per byte, for leads in
+// 0..3 and R in 1..8 (what __vsubus4(R * 0x01010101, leads) returns) without
+// the emulated SIMD instruction: R is raised by the bytes whose lead exceeds
+// it (lead 3 when R <= 2, lead >= 2 when R == 1) so the subtraction never
+// borrows across bytes.
+__device__ __forceinline__ uint32_t stored_counts(int R, uint32_t ldb) {
+    const uint32_t hi = (ldb >> 1) & 0x01010101u;   // lead >= 2
+    const uint32_t l3 = ldb & hi;                   // lead == 3
+    uint32_t up = R <= 2 ? l3 : 0u;
+    if (R <= 1) up += hi;
+    return (uint32_t)R * 0x01010101u + up - ldb;
+}
 __device__ __forceinline__ void split_reqlen(int reqLength, int* R, int* s) {
     int rb = reqLength & 7;
     *R = (reqLength >> 3) + (rb != 0);

@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kFxThreads) k_fxr_eval(const T* x, unsigned lo
 #pragma unroll
     for (int k = 0; k < NC; k++) {
         // min(lead, R) per value = R - max(R - lead, 0), bytewise
-        const uint32_t m = R4 - __vsubus4(R4, ldb[k]);
+        const uint32_t m = R4 - stored_counts(R, ldb[k]);
         const uint32_t keep = low_bytes_mask(len - 4 * (sl + k * G));
         lead += ((m & keep) * 0x01010101u) >> 24;
     }
