@@ -487,14 +487,17 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
         // warp 0: T_{j-1}'s look-back window, in flight until the next iteration
         if (warp == 0 && t1 >= 0) lo1 = window_load(fld(f1), t1);
         // every warp: the tile's block offsets (two warp-wide halves)
-        const bool in0 = lane < TB, in1 = lane + 32 < TB;
-        const uint32_t sz0 = in0 ? s_size[r][lane] : 0, sz1 = in1 ? s_size[r][lane + 32] : 0;
+        const bool in0 = lane < TB;
+        const uint32_t sz0 = in0 ? s_size[r][lane] : 0;
         const uint32_t i0 = warp_inclusive_sum(sz0);
-        const uint32_t c0 = __shfl_sync(0xffffffffu, i0, 31);
-        const uint32_t i1 = warp_inclusive_sum(sz1) + c0;
-        const uint32_t e0 = i0 - sz0, e1 = i1 - sz1;
-        const uint32_t loc_lo = __shfl_sync(0xffffffffu, e0, lb & 31);
-        const uint32_t loc_hi = __shfl_sync(0xffffffffu, e1, lb & 31);
+        const uint32_t loc_lo = __shfl_sync(0xffffffffu, i0 - sz0, lb & 31);
+        uint32_t i1 = i0, loc_hi = 0;   // tiles of up to 32 blocks have no second half
+        if constexpr (TB > 32) {
+            const bool in1 = lane + 32 < TB;
+            const uint32_t sz1 = in1 ? s_size[r][lane + 32] : 0;
+            i1 = warp_inclusive_sum(sz1) + __shfl_sync(0xffffffffu, i0, 31);
+            loc_hi = __shfl_sync(0xffffffffu, i1 - sz1, lb & 31);
+        }
         if (warp == 0) {
             const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
             if (lane == 0) s_agg[r] = agg;

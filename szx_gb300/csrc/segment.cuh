@@ -211,8 +211,11 @@ __device__ __forceinline__ void seg_minmax(const T (&v)[EncCfg<T>::E], int len, 
             if (mx == (T)0) mx = first;
         }
     }
-    const T x0 = __shfl_sync(0xffffffffu, v[0], 0, G);
-    if (isnan(x0)) { mn = x0; mx = x0; }
+    // a NaN first value pins both extremes; only a block holding a NaN can have one
+    if (__any_sync(0xffffffffu, special)) {
+        const T x0 = __shfl_sync(0xffffffffu, v[0], 0, G);
+        if (isnan(x0)) { mn = x0; mx = x0; }
+    }
 }
 
 
