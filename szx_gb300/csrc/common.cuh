@@ -639,66 +639,6 @@ __device__ __forceinline__ unsigned long long prefix_resolve(unsigned long long*
     return pa;
 }
 
-// The look-back above split in two, so that the first window's loads are in
-// flight while the warp does other work: lookback_load issues them,
-// prefix_resolve_pre starts from the loaded window (status words only move
-// forward -- none, aggregate, inclusive -- so an early read is still valid).
-struct LookbackWin {
-    unsigned long long w[4];
-};
-__device__ __forceinline__ void lookback_load(const unsigned long long* st, long long tile, LookbackWin& lw) {
-    const long long g = (((tile - 1) >> 2) << 2) - 4 * (long long)lane_id();
-    if (tile > 0 && g >= 0) ld_volatile_v2x2(st + g, lw.w);
-    else lw.w[0] = lw.w[1] = lw.w[2] = lw.w[3] = kS64Inc;
-}
-__device__ __forceinline__ unsigned long long prefix_resolve_pre(unsigned long long* st, long long tile,
-                                                                unsigned long long agg, int* err,
-                                                                const LookbackWin& lw) {
-    if (tile == 0) return 0;
-    const unsigned lane = lane_id();
-    unsigned long long pa = 0;
-    long long g0 = ((tile - 1) >> 2) << 2;
-    unsigned spins = 0;
-    bool failed = false, first = true;
-    while (true) {
-        const long long g = g0 - 4 * (long long)lane;
-        unsigned long long w[4];
-        if (first) {
-            w[0] = lw.w[0]; w[1] = lw.w[1]; w[2] = lw.w[2]; w[3] = lw.w[3];
-            first = false;
-        } else if (g >= 0) {
-            ld_volatile_v2x2(st + g, w);
-        } else {
-            w[0] = w[1] = w[2] = w[3] = kS64Inc;
-        }
-        int inc_j = -1;
-        bool ready = true;
-        unsigned long long sa = 0;
-#pragma unroll
-        for (int j = 3; j >= 0; j--) {
-            const unsigned long long f = w[j] & ~kS64Val;
-            if (g + j < tile && inc_j < 0) {
-                if (f == kS64Inc) { inc_j = j; sa += w[j] & kS64Val; }
-                else { ready = ready && f != 0; sa += w[j] & kS64Val; }
-            }
-        }
-        const unsigned inc_mask = __ballot_sync(0xffffffffu, inc_j >= 0);
-        const unsigned stop = inc_mask ? (unsigned)__ffs(inc_mask) - 1 : 31u;
-        const unsigned window = stop == 31u ? 0xffffffffu : ((1u << (stop + 1)) - 1);
-        if (__ballot_sync(0xffffffffu, !ready) & window) {
-            if (++spins > kSpinLimit) { failed = true; break; }
-            __nanosleep(spins < 64 ? 32 : 256);
-            continue;
-        }
-        pa += warp_sum(lane <= stop ? sa : 0ull);
-        if (inc_mask) break;
-        g0 -= 128;
-    }
-    if (failed && lane == 0) atomicExch(err, kErrLookback);
-    if (lane == 0) st_volatile64(&st[tile], kS64Inc | ((pa + agg) & kS64Val));
-    return pa;
-}
-
 // The look-back from a window of status words that a TMA bulk copy has put
 // in shared memory: win[i] holds the word of tile lo + i, for every tile in
 // [lo, tile).  Lane l reads the words of tiles tile-1-l-32k (k = 0..15, rows
