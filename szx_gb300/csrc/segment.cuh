@@ -229,15 +229,14 @@ __device__ __forceinline__ void seg_lead_bytes(const typename Elem<T>::U (&cur)[
     using U = typename Elem<T>::U;
     constexpr int NC = EncCfg<T>::E / 4;
     const int sl = (int)(lane_id() & (G - 1));
-    U last_prev = 0;
+    U wrap = 0;   // lane 0: the last lane's value of the previous round (zero before the block)
 #pragma unroll
     for (int k = 0; k < NC; k++) {
         // value before this chunk: the previous lane's chunk k, or for lane 0
-        // the last lane's chunk k-1 (zero before the block)
-        const U up = __shfl_up_sync(0xffffffffu, cur[4 * k + 3], 1, G);
-        const U wrap = __shfl_sync(0xffffffffu, last_prev, G - 1, G);
-        const U prev = sl ? up : (k ? wrap : (U)0);
-        last_prev = cur[4 * k + 3];
+        // the last lane's chunk k-1 -- one rotation per round serves both
+        const U rot = __shfl_sync(0xffffffffu, cur[4 * k + 3], (sl + G - 1) & (G - 1), G);
+        const U prev = sl ? rot : wrap;
+        wrap = rot;
         uint32_t b = 0;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
