@@ -2,8 +2,9 @@
  * CPU oracle for the SZx blocked codec -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference algorithm (szcompressor/SZx), used by
- * tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the
- * checker and as the timed CPU stand-in.  The product library never links,
+ * tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg: the
+ * oracle GPU results are compared with, and the timed CPU stand-in.  The
+ * product library never links,
  * loads or calls it.  Every function cites the reference file:line it follows.
  *
  * Parity of this restatement is pinned against the reference library itself,
