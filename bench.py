@@ -11,14 +11,26 @@ A step is one compress and one decompress of the whole field.
                CUDA events on the launching stream
   e2e        = the same metric through the reference-facing C entry points
                SZx_fast_compress_args / SZx_fast_decompress with host buffers
-               (pinned input; malloc'd outputs as the reference API returns),
-               host<->device copies inside the timed region (wall clock: the
-               calls are synchronous)
+               (pageable numpy input, as a drop-in caller passes it; malloc'd
+               outputs as the reference API returns them), host<->device
+               copies inside the timed region (wall clock: the calls are
+               synchronous)
   roofline   = the dominant kernel's algorithmic bytes per launch / its mean
                launch time (CUDA events the library records around each launch)
-               against the measured HBM copy bandwidth
+               against the measured HBM copy bandwidth; roofline_decode the
+               same for the decoder
+  stream_equal / decode_equal = after the timed region, the benchmarked
+               stream and decoded field compared byte for byte with the
+               oracle's
   cpu_baseline / --impl reference = the oracle's block-parallel (OpenMP) port of
                the reference codec on the host cores
+
+The same run adds the rest of the headline metric as extra keys (``--extras``,
+on by default at N=1): ``mode1`` (the same field through fastMode 1),
+``batched`` (mixed-size fields in one persistent launch replayed from a CUDA
+graph, against per-field launches) and ``fixed_rate`` (learned fixed-rate
+fields/s against plain bisection).  ``--workload c4`` / ``c5`` print those
+alone as their own line.
 
 Multi-GPU: replicas only (one independent field per rank), value summed.
 """
@@ -68,16 +80,17 @@ def read_peaks():
 
 
 def read_traffic(kernel: str):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
+    """(DRAM bytes per value, where that figure was measured) from the
+    committed ncu summary, or (None, None)."""
     p = os.path.join(ROOT, "profiles", "traffic.txt")
     if not os.path.exists(p):
-        return None
+        return None, None
     with open(p) as f:
         for line in f:
             parts = line.split()
             if len(parts) >= 3 and parts[0] == kernel and parts[1] == "bytes_per_element":
-                return float(parts[2])
-    return None
+                return float(parts[2]), " ".join(parts[3:]) or None
+    return None, None
 
 
 class ClockSampler:
@@ -124,6 +137,16 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+FIELD_SEED = 1234
+
+
+def common_config(wl, n, world):
+    """The `config` both arms print (same workload, size, seed and L2 note)."""
+    return {"workload": wl["desc"], "elements": int(n), "seed": FIELD_SEED,
+            "l2": f"inputs ({n * 4 >> 20} MiB) larger than L2; no flush needed",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+
 def make_field(wl, seed, device):
     import torch
 
@@ -159,7 +182,7 @@ def run_reference(args, wl, rank, world):
     if rank != 0:
         return
     dev = "cuda" if torch.cuda.is_available() else "cpu"
-    x = make_field(wl, 1234, dev).cpu().numpy()
+    x = make_field(wl, FIELD_SEED, dev).cpu().numpy()
     import oracle as O
     r = O.value_range(x)[0]
     eb = float(np.float32(np.float32(r) * np.float32(wl["rel"])))
@@ -177,7 +200,8 @@ def run_reference(args, wl, rank, world):
         "metric": "compress/decompress GB/s (fp32 REL 1e-3)", "value": round(val, 3), "unit": "GB/s",
         "impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded on-device FFT synthesis)", "config": {"workload": wl["desc"], "elements": x.size},
+        "data": "synthetic (seeded on-device FFT synthesis; no dataset ships with the reference)",
+        "config": common_config(wl, x.size, world),
         "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -201,6 +225,97 @@ def reduce_over_ranks(maxes, sums, device):
     return m.tolist(), s.tolist()
 
 
+def timed_steps(L, codec, x, y, sv, n, rel, steps, ev_stream_sync=True):
+    """`steps` compress+decompress steps of `codec` on field x (REL rel),
+    bracketed by CUDA events on the current stream, with the library's launch
+    trace on.  Returns (total ms, compress ms, decompress ms, {kernel: (ms, launches)})."""
+    import torch
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * steps)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    L.SZxG_trace_enable(1)
+    torch.cuda.synchronize()
+    t_start.record()
+    for k in range(steps):
+        ev[3 * k].record()
+        codec.compress(x, REL, 0.0, rel)
+        ev[3 * k + 1].record()
+        codec.decompress(sv, n, out=y)
+        ev[3 * k + 2].record()
+    t_end.record()
+    torch.cuda.synchronize()
+    names = C.create_string_buffer(4096)
+    tms = (C.c_double * 32)()
+    cnt = (C.c_ulonglong * 32)()
+    nk = L.SZxG_trace_collect(names, 4096, tms, cnt, 32)
+    L.SZxG_trace_enable(0)
+    kern = {nm: (tms[i], int(cnt[i])) for i, nm in enumerate(names.value.decode().split("\n")[:nk])}
+    tc = sum(ev[3 * k].elapsed_time(ev[3 * k + 1]) for k in range(steps))
+    td = sum(ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(steps))
+    return t_start.elapsed_time(t_end), tc, td, kern
+
+
+def kernel_roofline(kern, name, alg_bytes, peak, peak_kind, traffic=None):
+    """Roofline entry of one kernel: algorithmic bytes per launch / mean launch time."""
+    ms, cnt = kern[name]
+    achieved = alg_bytes / (ms / cnt / 1000) / 1e9
+    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
+            "algorithmic_bytes": int(alg_bytes), "ms_per_launch": round(ms / cnt, 5)}
+
+
+def prepare(codec, x, rel):
+    """One compress to learn where the stream lands (the same every step)."""
+    import szx_gb300 as S
+    codec.compress(x, REL, 0.0, rel)
+    info = codec.stream_info()
+    if info.status:
+        raise S.SZxError(info.status, "compress")
+    off, size = int(info.offset), int(info.size)
+    return info, off, size, codec.out[off:off + size]
+
+
+def run_mode1(args, L, x, rel, peak, peak_kind):
+    """The same field through the non-blocked layout (fastMode 1): GB/s,
+    kernel rooflines and stream equality with the oracle's serial mode 1."""
+    import numpy as np
+    import torch
+
+    import szx_gb300 as S
+    n = x.numel()
+    in_bytes = n * 4
+    codec = S.DeviceCodec(1, np.float32, n, 128)
+    y = torch.empty_like(x)
+    info, off, size, sv = prepare(codec, x, rel)
+    for _ in range(args.warmup):
+        codec.compress(x, REL, 0.0, rel)
+        codec.decompress(sv, n, out=y)
+    steps = max(3, args.steps // 2)
+    total, tc, td, kern = timed_steps(L, codec, x, y, sv, n, rel, steps)
+    got = sv.cpu().numpy().tobytes()
+    dec = y.cpu().numpy()
+    del codec, y
+    torch.cuda.empty_cache()
+    import oracle as O
+    xh = x.cpu().numpy()
+    want = O.fast_compress_args(1, xh, 1, 0.0, rel, 128)
+    equal = got == want
+    dec_equal = bool(equal and np.array_equal(dec.view(np.uint32),
+                                              O.decompress(1, np.float32, want, n).view(np.uint32)))
+    enc, decn = kern["nonblocked_encode"], kern["nonblocked_decode"]
+    return {
+        "workload": "the same 512^3 float32 field, REL 1e-3, fastMode 1 (non-blocked layout)",
+        "steps": steps, "value": round(2 * in_bytes * steps / ((tc + td) / 1000) / 1e9, 2), "unit": "GB/s",
+        "compress_gbs": round(in_bytes * steps / (tc / 1000) / 1e9, 2),
+        "decompress_gbs": round(in_bytes * steps / (td / 1000) / 1e9, 2),
+        "stream_bytes": size, "ratio": round(in_bytes / size, 4),
+        "kernels_ms_per_step": {k: round(v[0] / steps, 4) for k, v in kern.items()},
+        "roofline_encode": kernel_roofline(kern, "nonblocked_encode", in_bytes + size, peak, peak_kind),
+        "roofline_decode": kernel_roofline(kern, "nonblocked_decode", in_bytes + size, peak, peak_kind),
+        "stream_equal": equal, "decode_equal": dec_equal,
+        "gpu_launches": sum(c for _, c in kern.values()),
+    }
+
+
 def run_ours(args, wl, rank, world, local_rank):
     import numpy as np
     import torch
@@ -213,56 +328,24 @@ def run_ours(args, wl, rank, world, local_rank):
         import torch.distributed as D
     torch.cuda.set_device(local_rank)
     L = lib()
-    x = make_field(wl, 1234 + rank, "cuda")
+    x = make_field(wl, FIELD_SEED + rank, "cuda")
     n = x.numel()
     in_bytes = n * 4
     mode, bs, rel = wl["mode"], wl["bs"], wl["rel"]
     codec = S.DeviceCodec(mode, np.float32, n, bs)
     y = torch.empty_like(x)
-
-    # one step to learn where the stream lands (same input every step)
-    codec.compress(x, REL, 0.0, rel)
-    info = codec.stream_info()
-    assert info.status == 0, S.SZxError(info.status, "compress")
-    off, size = int(info.offset), int(info.size)
-    sv = codec.out[off:off + size]
-
-    def step(ev=None, k=0):
-        if ev:
-            ev[3 * k].record()
-        codec.compress(x, REL, 0.0, rel)
-        if ev:
-            ev[3 * k + 1].record()
-        codec.decompress(sv, n, out=y)
-        if ev:
-            ev[3 * k + 2].record()
+    info, off, size, sv = prepare(codec, x, rel)
 
     for _ in range(args.warmup):
-        step()
+        codec.compress(x, REL, 0.0, rel)
+        codec.decompress(sv, n, out=y)
     torch.cuda.synchronize()
     if dist:
         D.barrier()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
-    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(local_rank) if rank == 0 else None
     time.sleep(0.3)
-    L.SZxG_trace_enable(1)
-    torch.cuda.synchronize()
-    t_start.record()
-    for k in range(args.steps):
-        step(ev, k)
-    t_end.record()
-    torch.cuda.synchronize()
+    total_ms, tc, td, kern = timed_steps(L, codec, x, y, sv, n, rel, args.steps)
     clk = clocks.stop() if clocks else None
-    names = C.create_string_buffer(4096)
-    tms = (C.c_double * 32)()
-    cnt = (C.c_ulonglong * 32)()
-    nk = L.SZxG_trace_collect(names, 4096, tms, cnt, 32)
-    L.SZxG_trace_enable(0)
-    kern = {nm: (tms[i], int(cnt[i])) for i, nm in enumerate(names.value.decode().split("\n")[:nk])}
-    total_ms = t_start.elapsed_time(t_end)
-    tc = sum(ev[3 * k].elapsed_time(ev[3 * k + 1]) for k in range(args.steps))
-    td = sum(ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(args.steps))
     launches = sum(c for _, c in kern.values())
     info2 = codec.stream_info()
     assert (int(info2.offset), int(info2.size), info2.status) == (off, size, 0)
@@ -272,19 +355,19 @@ def run_ours(args, wl, rank, world, local_rank):
     err = (x.double() - y.double()).abs()
     ulp = torch.nextafter(x.abs(), torch.full_like(x, float("inf"))) - x.abs()
     bound_ok = bool((err <= eb + 2 * ulp.double()).all().item())
+    del err, ulp
 
     if dist:
         (total_ms, tc, td), (launches,) = reduce_over_ranks([total_ms, tc, td], [launches], "cuda")
         launches = int(launches)
 
-    # ---- e2e through the reference-facing entry points, host buffers
-    xh = torch.empty(n, dtype=torch.float32, pin_memory=True)
-    xh.copy_(x.cpu())
+    # ---- e2e through the reference-facing entry points, pageable host buffers
+    xh = x.cpu().numpy()                       # ordinary (pageable) host memory, as a drop-in caller has
     free = libc().free
     sz = C.c_size_t()
 
     def e2e_step():
-        p = L.SZx_fast_compress_args(mode, 0, C.c_void_p(xh.data_ptr()), C.byref(sz), REL, 0.0, rel, 0.0, 0.0,
+        p = L.SZx_fast_compress_args(mode, 0, C.c_void_p(xh.ctypes.data), C.byref(sz), REL, 0.0, rel, 0.0, 0.0,
                                      0, 0, 0, 0, n)
         if not p:
             raise S.SZxError(S.api.last_error(), "SZx_fast_compress_args")
@@ -312,29 +395,40 @@ def run_ours(args, wl, rank, world, local_rank):
     K = args.steps
     value = world * 2 * in_bytes * K / ((tc + td) / 1000) / 1e9
     peak, peak_kind = read_peaks()
-    # dominant kernel and its roofline
     enc = "blocked_encode" if mode != 1 else "nonblocked_encode"
     dec = "blocked_decode" if mode != 1 else "nonblocked_decode"
     dom = max((enc, dec), key=lambda k: kern.get(k, (0, 0))[0])
-    dms, dcnt = kern[dom]
     alg = in_bytes + size          # encode: read field, write stream; decode: read stream, write field
-    achieved = alg / (dms / dcnt / 1000) / 1e9
-    tb = read_traffic(dom)
-    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                "traffic": round(tb * n) if tb else None, "algorithmic_bytes": alg}
-    # CPU baseline: the same field on the host cores
-    x_np = x.cpu().numpy()
+    tb, tb_note = read_traffic(dom)
+    roofline = kernel_roofline(kern, dom, alg, peak, peak_kind, round(tb * n) if tb else None)
+    if tb:
+        roofline["traffic_source"] = tb_note
+    other = dec if dom == enc else enc
+    roofline_other = kernel_roofline(kern, other, alg, peak, peak_kind)
+
+    # parity of what was timed: the stream and the decoded field against the
+    # oracle's block-parallel port of the reference codec (outside the timing)
+    import oracle as O
+    got = sv.cpu().numpy()
     threads = os.cpu_count() or 1
-    cpu_val, _ = cpu_codec_gbs(x_np, eb, bs, 2, threads)
+    want, wlen = O.compress_m3_omp(xh, np.float32(eb), bs, threads=threads) if mode == 3 else (None, 0)
+    stream_equal = bool(mode == 3 and wlen == size and np.array_equal(got, want[:wlen]))
+    decode_equal = bool(stream_equal and np.array_equal(
+        y.cpu().numpy().view(np.uint32),
+        O.decompress_m3_omp(np.float32, want, wlen, n, threads=threads).view(np.uint32)))
+    del want, got
+    del codec, y
+    torch.cuda.empty_cache()
+
+    # CPU baseline: the same field on the host cores
+    cpu_val, _ = cpu_codec_gbs(xh, eb, bs, 2, threads)
     line = {
         "metric": "compress/decompress GB/s (fp32 REL 1e-3)",
         "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": round(total_ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded on-device FFT synthesis; no dataset ships with the reference)",
-        "config": {"workload": wl["desc"], "elements": n, "stream_bytes": size, "ratio": round(in_bytes / size, 4),
-                   "bound": eb, "l2": f"inputs ({in_bytes >> 20} MiB) larger than L2; no flush needed",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": common_config(wl, n, world),
+        "stream_bytes": size, "ratio": round(in_bytes / size, 4), "bound": eb,
         "compress_gbs": round(world * in_bytes * K / (tc / 1000) / 1e9, 2),
         # the REL range pass hoisted out, as the reference CLI converts REL to ABS first
         "compress_codec_only_gbs": round(world * in_bytes * K / ((tc - kern.get("range", (0.0, 0))[0]) / 1000) / 1e9,
@@ -343,14 +437,24 @@ def run_ours(args, wl, rank, world, local_rank):
         "kernels_ms_per_step": {k: round(v[0] / K, 4) for k, v in kern.items()},
         "gpu_launches": launches,
         "bound_ok": bound_ok,
+        "stream_equal": stream_equal,
+        "decode_equal": decode_equal,
         "clocks": clk,
         "e2e": {"value": round(world * 2 * in_bytes / e2e_s / 1e9, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": in_bytes + size, "d2h_bytes_per_step": size + in_bytes,
-                "api": "SZx_fast_compress_args + SZx_fast_decompress (host buffers)"},
+                "api": "SZx_fast_compress_args + SZx_fast_decompress (pageable host input)"},
         "roofline": roofline,
+        "roofline_" + ("decode" if other == dec else "encode"): roofline_other,
         "cpu_baseline": {"value": round(cpu_val, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": f"the same field ({n} float32 values), compress+decompress, best of 2"},
     }
+    if args.extras and world == 1 and mode == 3:
+        line["mode1"] = run_mode1(args, L, x, rel, peak, peak_kind)
+        del x
+        torch.cuda.empty_cache()
+        line["batched"] = run_batched(args, WORKLOADS["c4"], fields=args.extra_fields)
+        torch.cuda.empty_cache()
+        line["fixed_rate"] = run_fixed_rate(args, WORKLOADS["c5"])
     print(json.dumps(line), flush=True)
 
 
@@ -358,37 +462,8 @@ def make_batch_fields(nf, seed, device):
     """C4 fields on the device: sizes log-uniform 2^14..2^26, each a seeded
     1-D spectral field (k^-5/3), piecewise-constant levels or white noise,
     with an ABS bound log-uniform in 1e-5..1e-2 of its range."""
-    import numpy as np
-    import torch
-    rng = np.random.default_rng(seed)
-    sizes = np.exp(rng.uniform(np.log(2 ** 14), np.log(2 ** 26), nf)).astype(np.int64)
-    kinds = rng.integers(0, 3, nf)
-    scales = 10.0 ** rng.uniform(-5, -2, nf)
-    g = torch.Generator(device=device).manual_seed(seed)
-    xs, ebs = [], []
-    for n, kind, sc in zip(sizes, kinds, scales):
-        n = int(n)
-        if kind == 0:   # synthesised at the next power of two, then truncated
-            n2 = 1 << (n - 1).bit_length()
-            nf_ = n2 // 2 + 1
-            k = torch.arange(nf_, device=device, dtype=torch.float32)
-            k[0] = 1.0
-            amp = k ** (-5.0 / 6.0)
-            amp[0] = 0.0
-            z = torch.complex(torch.randn(nf_, generator=g, device=device),
-                              torch.randn(nf_, generator=g, device=device)) * amp
-            x = torch.fft.irfft(z, n=n2)[:n]
-            x = (x - x.mean()) / (x.std() + 1e-30)
-        elif kind == 1:
-            run = int(rng.integers(64, 4096))
-            x = torch.repeat_interleave(torch.randn(n // run + 1, generator=g, device=device), run)[:n].contiguous()
-        else:
-            x = torch.randn(n, generator=g, device=device)
-        x = x.float().contiguous()
-        r = float((x.max() - x.min()).item()) or 1.0
-        xs.append(x)
-        ebs.append(float(r * sc))
-    return xs, ebs
+    from szx_gb300 import synth
+    return synth.batch_fields(nf, seed, 14, 26, device)
 
 
 def run_fixed_rate(args, wl):
@@ -457,10 +532,10 @@ def run_fixed_rate(args, wl):
                      "corpus_s": round(t1 - t0, 1), "train_s": round(t2 - t1, 2)},
         "clocks": clk,
     }
-    print(json.dumps(line))
+    return line
 
 
-def run_batched(args, wl):
+def run_batched(args, wl, fields=None):
     """C4: one batch (one persistent launch per kernel, replayed from a CUDA
     graph) against the same fields compressed by per-field calls."""
     import numpy as np
@@ -479,7 +554,8 @@ def run_batched(args, wl):
     L.SZxG_batch_status.argtypes = [C.c_void_p, C.c_void_p]
     L.SZxG_batch_destroy.argtypes = [C.c_void_p]
     mode, bs = wl["mode"], wl["bs"]
-    xs, ebs = make_batch_fields(args.fields, 4242, "cuda")
+    nfields = fields or args.fields
+    xs, ebs = make_batch_fields(nfields, 4242, "cuda")
     nf = len(xs)
     total_in = sum(x.numel() for x in xs) * 4
     outs, fields = [], (Field * nf)()
@@ -625,7 +701,7 @@ def run_batched(args, wl):
                        "fields_over_bound": bad},
         "clocks": clk,
     }
-    print(json.dumps(line))
+    return line
 
 
 def main():
@@ -636,6 +712,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--fields", type=int, default=2000, help="c4: number of fields")
+    ap.add_argument("--extras", dest="extras", action="store_true", default=True,
+                    help="c2 at N=1: add the mode1, batched and fixed_rate keys (default)")
+    ap.add_argument("--no-extras", dest="extras", action="store_false")
+    ap.add_argument("--extra-fields", type=int, default=2000, help="fields of the batched extra key")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -643,13 +723,18 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
+        if "rel" not in wl:
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": f"no CPU arm for workload {args.workload}; "
+                                  "the reference arm times the single-field codec"}), flush=True)
+            return
         run_reference(args, wl, rank, world)
         return
     if args.workload == "c4":
-        run_batched(args, wl)
+        print(json.dumps(run_batched(args, wl)), flush=True)
         return
     if args.workload == "c5":
-        run_fixed_rate(args, wl)
+        print(json.dumps(run_fixed_rate(args, wl)), flush=True)
         return
     if world > 1:
         import torch

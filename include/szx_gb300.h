@@ -52,8 +52,10 @@ unsigned char* SZx_fast_compress_args(int fastMode, int dataType, void* data, si
                                       float absErrBound, float relBoundRatio, float compressionRatio, float tolerance,
                                       size_t r5, size_t r4, size_t r3, size_t r2, size_t r1);
 
-/* szx/include/szx.h:78, szx/src/szx.cc:378-430.  fastMode 1, 3, 4.  Returns a
- * malloc'd array of SZx_computeDataLength(r5..r1) values. */
+/* szx/include/szx.h:78, szx/src/szx.cc:378-430.  fastMode 1, 2, 3, 4 (the
+ * reference's dispatcher decodes 1, 3, 4; fastMode 2 streams, which FXR
+ * produces, are decoded here too).  Returns a malloc'd array of
+ * SZx_computeDataLength(r5..r1) values. */
 void* SZx_fast_decompress(int fastMode, int dataType, unsigned char* bytes, size_t byteLength, size_t r5, size_t r4,
                           size_t r3, size_t r2, size_t r1);
 
@@ -156,7 +158,9 @@ int SZxG_workspace_status(const void* d_workspace, void* stream);
  * SZXG_ERR_TOO_LARGE before any GPU work.  All calls on a device share the
  * array: calls that overlap on the GPU race, so order them on one stream.
  * The first call on a device resolves the array's address; make it before
- * any stream capture.  Output, info and errors as SZxG_compress. */
+ * any stream capture.  Output and info as SZxG_compress; the same error codes,
+ * plus SZXG_ERR_UNSUPPORTED for fastMode 1 and SZXG_ERR_TOO_LARGE beyond the
+ * limit; every return sets SZxG_get_last_error(). */
 int SZxG_compress_noalloc(int fastMode, int dataType, const void* d_data, size_t nbEle, int blockSize,
                           int errBoundMode, float absErrBound, float relBoundRatio, void* d_out, size_t outCapacity,
                           SZxG_StreamInfo* d_info, void* stream);
@@ -262,6 +266,16 @@ int SZxG_batch_fixed_rate(SZxG_Batch* batch, const SZxG_Mlp* mlp, const float* t
  * collect() waits for the recorded events and writes, per kernel name, the
  * summed milliseconds and launch count; names are '\n'-separated in `names`.
  * Returns the number of kernels reported. */
+/* Failure detection (no counterpart in the reference): runs the device-wide
+ * look-back the codecs use to place variable-length payloads (scan 0: the
+ * encoders' 64-bit status words; scan 1: the decoders' 32-bit words) over
+ * ntiles (<= 4096) one-warp tiles, tile t contributing t + 1, with tile
+ * `withheld` (-1: none) never publishing, and waits bounded by spinLimit
+ * polls.  Returns SZXG_ERR_LOOKBACK when a wait gave up, else SZXG_OK with
+ * prefix[t] = t(t+1)/2 (host array of ntiles, may be NULL).  Synchronous. */
+int SZxG_selftest_lookback(int scan, int ntiles, int withheld, unsigned spinLimit, unsigned long long* prefix,
+                           void* stream);
+
 void SZxG_trace_enable(int on);
 int SZxG_trace_collect(char* names, size_t names_len, double* ms, unsigned long long* counts, int max_kernels);
 

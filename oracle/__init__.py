@@ -17,7 +17,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libszxref.so")
-REF_SRC = "/root/reference"
+# Where the reference's sources are read from, when they are on this machine:
+# the SZX_REFERENCE_SRC environment variable, else the path the build recipe
+# (__graft_entry__.build) passes in.  No default: without it only the
+# restatement is built.
+REF_SRC = os.environ.get("SZX_REFERENCE_SRC", "")
 
 FLOAT, DOUBLE = 0, 1
 _u8p = C.POINTER(C.c_uint8)
@@ -25,11 +29,13 @@ _lib = None
 _ref = None
 
 
-def build(reference: bool = True) -> None:
-    """Compile liboracle.so, and the reference library when its sources exist."""
+def build(reference: bool = True, reference_src: str | None = None) -> None:
+    """Compile liboracle.so, and the reference library when its sources exist
+    (at `reference_src`, else SZX_REFERENCE_SRC)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if reference and os.path.isdir(os.path.join(REF_SRC, "szx", "src")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+    src = reference_src or REF_SRC
+    if reference and src and os.path.isdir(os.path.join(src, "szx", "src")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
 
 
 def lib() -> C.CDLL:

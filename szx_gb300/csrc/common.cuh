@@ -195,7 +195,10 @@ __device__ __forceinline__ uint32_t ld_acquire32(const uint32_t* p) {
 constexpr unsigned long long kFlagAgg = 1ull << 62;
 constexpr unsigned long long kFlagInc = 2ull << 62;
 constexpr unsigned long long kValMask = (1ull << 62) - 1;
-constexpr unsigned kSpinLimit = 1u << 22;   // polls before giving up (~seconds with backoff)
+constexpr unsigned kSpinLimit = 1u << 22;   // polls before giving up (~1 s with backoff)
+// Every look-back below takes its poll limit as a last argument (default
+// kSpinLimit); the failure-detection self-test (selftest.cu) passes a small
+// one and withholds a tile, so the give-up path runs for real.
 
 enum : int { kErrNone = 0, kErrLookback = 1, kErrCapacity = 2, kErrStream = 3 };
 
@@ -236,7 +239,7 @@ struct Max3x21Op {
 template <typename Op = SumOp>
 __device__ __forceinline__ void lookback(TileStatus st, long long tile, unsigned long long a,
                                          unsigned long long b, unsigned long long* ex_a,
-                                         unsigned long long* ex_b, int* err) {
+                                         unsigned long long* ex_b, int* err, unsigned limit = kSpinLimit) {
     const unsigned lane = lane_id();
     if (tile == 0) {
         if (lane == 0) {
@@ -269,7 +272,7 @@ __device__ __forceinline__ void lookback(TileStatus st, long long tile, unsigned
         unsigned window = stop == 31u ? 0xffffffffu : ((1u << (stop + 1)) - 1);
         unsigned not_ready = __ballot_sync(0xffffffffu, flag == 0) & window;
         if (not_ready) {
-            if (++spins > kSpinLimit) { failed = true; break; }
+            if (++spins > limit) { failed = true; break; }
             __nanosleep(spins < 64 ? 32 : 256);
             continue;
         }
@@ -397,7 +400,8 @@ struct WriterPolicy {
 // Returns the exclusive prefixes.
 template <typename Policy = SumPolicy>
 __device__ __forceinline__ void lookback_wide(TileStatus32 s, long long tile, uint32_t agg_a, uint32_t agg_b,
-                                              unsigned long long* ex_a, unsigned long long* ex_b, int* err) {
+                                              unsigned long long* ex_a, unsigned long long* ex_b, int* err,
+                                              unsigned limit = kSpinLimit) {
     const unsigned lane = lane_id();
     const uint32_t packed = (agg_b << 23) | (agg_a & 0x7FFFFFu);
     const unsigned long long self_b = Policy::contrib(agg_b, tile);
@@ -451,7 +455,7 @@ __device__ __forceinline__ void lookback_wide(TileStatus32 s, long long tile, ui
         const unsigned stop = inc_mask ? (unsigned)__ffs(inc_mask) - 1 : 31u;
         const unsigned window = stop == 31u ? 0xffffffffu : ((1u << (stop + 1)) - 1);
         if (__ballot_sync(0xffffffffu, !ready) & window) {
-            if (++spins > kSpinLimit) { failed = true; break; }
+            if (++spins > limit) { failed = true; break; }
             __nanosleep(spins < 64 ? 32 : 256);
             continue;
         }
@@ -497,7 +501,8 @@ __device__ __forceinline__ void lookback_publish(TileStatus32 s, long long tile,
 // Whole warp; the tile's aggregate must already be published.
 template <typename Policy = SumPolicy>
 __device__ __forceinline__ void lookback_resolve(TileStatus32 s, long long tile, uint32_t agg_a, uint32_t agg_b,
-                                                 unsigned long long* ex_a, unsigned long long* ex_b, int* err) {
+                                                 unsigned long long* ex_a, unsigned long long* ex_b, int* err,
+                                                 unsigned limit = kSpinLimit) {
     const unsigned lane = lane_id();
     if (tile == 0) {
         *ex_a = 0;
@@ -542,7 +547,7 @@ __device__ __forceinline__ void lookback_resolve(TileStatus32 s, long long tile,
         const unsigned stop = inc_mask ? (unsigned)__ffs(inc_mask) - 1 : 31u;
         const unsigned window = stop == 31u ? 0xffffffffu : ((1u << (stop + 1)) - 1);
         if (__ballot_sync(0xffffffffu, !ready) & window) {
-            if (++spins > kSpinLimit) { failed = true; break; }
+            if (++spins > limit) { failed = true; break; }
             __nanosleep(spins < 64 ? 32 : 256);
             continue;
         }
@@ -599,7 +604,8 @@ __device__ __forceinline__ void prefix_publish(unsigned long long* st, long long
 // Whole warp: exclusive prefix of `tile` (aggregate already published), then
 // publish its inclusive value.  `st` holds ntiles + 4 zeroed words.
 __device__ __forceinline__ unsigned long long prefix_resolve(unsigned long long* st, long long tile,
-                                                            unsigned long long agg, int* err) {
+                                                            unsigned long long agg, int* err,
+                                                            unsigned limit = kSpinLimit) {
     if (tile == 0) return 0;
     const unsigned lane = lane_id();
     unsigned long long pa = 0;
@@ -626,7 +632,7 @@ __device__ __forceinline__ unsigned long long prefix_resolve(unsigned long long*
         const unsigned stop = inc_mask ? (unsigned)__ffs(inc_mask) - 1 : 31u;
         const unsigned window = stop == 31u ? 0xffffffffu : ((1u << (stop + 1)) - 1);
         if (__ballot_sync(0xffffffffu, !ready) & window) {
-            if (++spins > kSpinLimit) { failed = true; break; }
+            if (++spins > limit) { failed = true; break; }
             __nanosleep(spins < 64 ? 32 : 256);
             continue;
         }

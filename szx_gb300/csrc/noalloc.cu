@@ -90,20 +90,31 @@ Workspace carve(unsigned char* b) {
 
 using namespace szxg;
 
+namespace {
+int na_ret(int rc) {
+    set_last_error(rc);
+    return rc;
+}
+}  // namespace
+
 extern "C" int SZxG_compress_noalloc(int fastMode, int dataType, const void* d_data, size_t nbEle, int blockSize,
                                      int errBoundMode, float absErrBound, float relBoundRatio, void* d_out,
                                      size_t outCapacity, SZxG_StreamInfo* d_info, void* stream) {
+    // Same codes as SZxG_compress, plus SZXG_ERR_UNSUPPORTED for fastMode 1
+    // (no blocks: this entry point has no non-blocked variant) and
+    // SZXG_ERR_TOO_LARGE beyond the fixed scratch.  Every return sets the
+    // thread's last error.
     if (fastMode != kBlocked && fastMode != kRandomAccess && fastMode != kRandomAccessNative)
-        return SZXG_ERR_UNSUPPORTED;
+        return na_ret(fastMode == kNonBlocked ? SZXG_ERR_UNSUPPORTED : SZXG_ERR_ARG);
     if (!d_data || !d_out || !d_info || nbEle == 0 || (dataType != 0 && dataType != 1) || blockSize < 1 ||
         blockSize > 256 || (fastMode == kBlocked && blockSize > 255) || (errBoundMode != ABS && errBoundMode != REL))
-        return SZXG_ERR_ARG;
+        return na_ret(SZXG_ERR_ARG);
     const size_t nb = (nbEle + (size_t)blockSize - 1) / (size_t)blockSize;
-    if (nb > kNoAllocMaxBlocks) return SZXG_ERR_TOO_LARGE;
-    if (outCapacity < blocked_bound(fastMode, dataType, nbEle, blockSize)) return SZXG_ERR_CAPACITY;
+    if (nb > kNoAllocMaxBlocks) return na_ret(SZXG_ERR_TOO_LARGE);
+    if (outCapacity < blocked_bound(fastMode, dataType, nbEle, blockSize)) return na_ret(SZXG_ERR_ARG);
     void* base = nullptr;
     int rc = scratch_address(&base);
-    if (rc) return rc;
+    if (rc) return na_ret(rc);
     Workspace ws = carve((unsigned char*)base);
     cudaStream_t s = (cudaStream_t)stream;
     const bool rel = errBoundMode == REL;
@@ -116,7 +127,7 @@ extern "C" int SZxG_compress_noalloc(int fastMode, int dataType, const void* d_d
         e = cudaMemcpyAsync(d_info, ws.result, sizeof(StreamResult), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return SZXG_ERR_CUDA;
+        return na_ret(SZXG_ERR_CUDA);
     }
-    return SZXG_OK;
+    return na_ret(SZXG_OK);
 }

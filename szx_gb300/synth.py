@@ -11,6 +11,9 @@ No dataset ships with the reference; these stand in for it:
 * ``trend_field``     -- the spectral field scaled by 1e6, plus a seeded linear
   trend, with 1% of values replaced by N(0,1e8) outliers (float64).
 * ``mixed_field``     -- one of spectral / piecewise-constant / white noise.
+* ``batch_fields``    -- many fields of log-uniform sizes, each spectral (1-D
+  k^-5/3), piecewise-constant or white noise, with an ABS bound log-uniform
+  in 1e-5..1e-2 of its range (the mixed-size batch workload).
 """
 from __future__ import annotations
 
@@ -102,3 +105,42 @@ def mixed_field(n: int, seed: int, device="cuda") -> torch.Tensor:
         levels = torch.randn((n + seg - 1) // seg, generator=g, device=device)
         return levels.repeat_interleave(seg)[:n].contiguous()
     return torch.randn(n, generator=g, device=device)
+
+
+def batch_fields(nf: int, seed: int, lo_exp: float = 14, hi_exp: float = 26, device="cuda",
+                 dtype=torch.float32):
+    """nf fields with sizes log-uniform in [2^lo_exp, 2^hi_exp], each a seeded
+    1-D k^-5/3 spectral field (unit variance), piecewise-constant levels (runs
+    of 64..4095) or white noise, and per-field ABS bounds log-uniform in
+    1e-5..1e-2 of the field's range (computed in float32).  Returns
+    (fields, bounds)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(2.0 ** lo_exp), np.log(2.0 ** hi_exp), nf)).astype(np.int64)
+    kinds = rng.integers(0, 3, nf)
+    scales = 10.0 ** rng.uniform(-5, -2, nf)
+    g = torch.Generator(device=device).manual_seed(seed)
+    xs, ebs = [], []
+    for n, kind, sc in zip(sizes, kinds, scales):
+        n = int(n)
+        if kind == 0:   # synthesised at the next power of two, then truncated
+            n2 = 1 << (n - 1).bit_length()
+            nh = n2 // 2 + 1
+            k = torch.arange(nh, device=device, dtype=torch.float32)
+            k[0] = 1.0
+            amp = k ** (-5.0 / 6.0)
+            amp[0] = 0.0
+            z = torch.complex(torch.randn(nh, generator=g, device=device),
+                              torch.randn(nh, generator=g, device=device)) * amp
+            x = torch.fft.irfft(z, n=n2)[:n]
+            x = (x - x.mean()) / (x.std() + 1e-30)
+        elif kind == 1:
+            run = int(rng.integers(64, 4096))
+            x = torch.repeat_interleave(torch.randn(n // run + 1, generator=g, device=device), run)[:n].contiguous()
+        else:
+            x = torch.randn(n, generator=g, device=device)
+        x = x.to(dtype).contiguous()
+        r = float((x.max() - x.min()).item()) or 1.0
+        xs.append(x)
+        ebs.append(float(np.float32(r * sc)))
+    return xs, ebs

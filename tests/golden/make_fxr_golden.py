@@ -40,8 +40,8 @@ def bits(v) -> int:
 
 def main():
     if O.reference() is None:
-        O.build(reference=True)
-    assert O.reference() is not None, "reference library not built (make -C oracle ref)"
+        O.build(reference=True, reference_src=os.environ.get("SZX_REFERENCE_SRC"))
+    assert O.reference() is not None, "reference library not built: set SZX_REFERENCE_SRC to the reference source tree"
     out = []
     for dt in (np.float32, np.float64):
         for name in F.FIELDS:

@@ -176,8 +176,8 @@ def run_reference(c):
 
 def main():
     if O.reference() is None:
-        O.build(reference=True)
-    assert O.reference() is not None, "reference library not built (make -C oracle ref)"
+        O.build(reference=True, reference_src=os.environ.get("SZX_REFERENCE_SRC"))
+    assert O.reference() is not None, "reference library not built: set SZX_REFERENCE_SRC to the reference source tree"
     manifest, arrays = [], {}
     for c in cases():
         res, why = run_reference(c)

@@ -244,3 +244,29 @@ def test_batch_decompress_isolates_bad_streams_and_replays(env):
         assert [i.status for i in infos] == [0, 3, 3, 0, 0]
         for k in (0, 3, 4):
             assert _same(outs[k], _single_decompress(env, 3, streams[k], sizes[k], 128, torch.float32)), k
+
+
+@pytest.mark.parametrize("mode,dtname,bs", [(3, "float32", 128), (3, "float64", 64)])
+def test_batch_streams_and_decodes_match_the_oracle(env, mode, dtname, bs):
+    """64 fields drawn like the mixed-size batch workload (sizes log-uniform
+    2^14..2^22, spectral / piecewise-constant / white noise, ABS bound
+    log-uniform 1e-5..1e-2 x range): every batched stream equals the oracle's
+    stream of that field (szx/src/szx_float.cc:1407-1489, double
+    szx/src/szx_double.cc:1509-1590) byte for byte, and the batched decode
+    equals the oracle's decode bit for bit."""
+    import oracle as O
+    from szx_gb300 import synth
+    torch = env[0]
+    dt = getattr(torch, dtname)
+    xs, ebs = synth.batch_fields(64, 2024 + bs, 14, 22, "cuda", dt)
+    got = _batch(env, mode, xs, bs, ebs)
+    hosts = [x.cpu().numpy() for x in xs]
+    for k, (xh, eb) in enumerate(zip(hosts, ebs)):
+        assert got[k] == O.compress(mode, xh, eb, bs), (k, xh.size)
+    streams = [torch.tensor(np.frombuffer(s, np.uint8).copy(), device="cuda") for s in got]
+    outs, infos, st = _batch_decompress(env, mode, streams, [x.numel() for x in xs], bs, dt)
+    assert st == 0
+    it = np.uint32 if dt == torch.float32 else np.uint64
+    for k, xh in enumerate(hosts):
+        z = O.decompress(mode, xh.dtype, got[k], xh.size)
+        assert np.array_equal(outs[k].cpu().numpy().view(it), z.view(it)), (k, xh.size)

@@ -75,6 +75,22 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls_in_a_row(env):
     assert a == b and len(a) > 20
     a, b = _run(env, 4, second, 64, 0, 1e-4, 0.0)
     assert a == b and len(a) > 20
+    # call 3: smaller again, a block count that is not a multiple of the tile,
+    # after a larger call left its contents in the shared array
+    third = (torch.randn(77_777, generator=g, device="cuda") * 3).contiguous()
+    a, b = _run(env, 3, third, 128, 0, 1e-2, 0.0)
+    assert a == b and len(a) > 20
+    torch_, L, _ = env
+    assert L.SZxG_get_last_error() == 0
+
+
+def test_noalloc_at_its_full_block_count(env):
+    torch = env[0]
+    g = torch.Generator(device="cuda").manual_seed(9)
+    n = MAX_BLOCKS * 8 - 3            # exactly MAX_BLOCKS blocks of 8 values, the last one short
+    x = (torch.randn(n, generator=g, device="cuda").cumsum(0) * 1e-3).contiguous()
+    a, b = _run(env, 3, x, 8, 0, 1e-3, 0.0)
+    assert a == b and len(a) > 20
 
 
 def test_noalloc_rejects_inputs_beyond_its_scratch(env):
@@ -87,4 +103,9 @@ def test_noalloc_rejects_inputs_beyond_its_scratch(env):
                                  C.c_void_p(out.data_ptr()), 1 << 40, C.c_void_p(info.data_ptr()),
                                  C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == 7
+    assert L.SZxG_get_last_error() == 7
     assert b"fixed scratch" in L.SZxG_error_string(rc)
+    rc = L.SZxG_compress_noalloc(1, 0, C.c_void_p(x.data_ptr()), 16, 128, 0, 1e-3, 0.0,
+                                 C.c_void_p(out.data_ptr()), 1 << 20, C.c_void_p(info.data_ptr()),
+                                 C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 6 and L.SZxG_get_last_error() == 6
