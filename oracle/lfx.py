@@ -55,13 +55,19 @@ def _lead(x: np.ndarray) -> np.ndarray:
     return np.where(x < (1 << 8), 3, np.where(x < (1 << 16), 2, np.where(x < (1 << 24), 1, 0)))
 
 
-def _blocks(x: np.ndarray):
-    """(sampled blocks [ns, 128], radius, median, sampled range) as the codec computes them."""
+OFF2 = 5   # the second sample: full blocks 5, 15, 25, ...
+
+
+def _blocks(x: np.ndarray, off: int = 0):
+    """(sampled blocks [ns, 128], radius, median, sampled range) as the codec
+    computes them; off 0: every 10th full block from block 0 (the range is
+    always this sample's), off OFF2: the second, disjoint sample."""
     x = np.ascontiguousarray(x, dtype=np.float32)
     full = x.size // BS
     ns = -(-full // RATE)
-    blk = x[: full * BS].reshape(full, BS)[np.arange(ns) * RATE]
-    fin = blk[np.isfinite(blk)]
+    blk0 = x[: full * BS].reshape(full, BS)[np.arange(ns) * RATE]
+    fin = blk0[np.isfinite(blk0)]
+    blk = blk0 if off == 0 else x[: full * BS].reshape(full, BS)[np.arange(off, full, RATE)]
     rng = np.float32(fin.max() - fin.min()) if fin.size else np.float32(0.0)
     mn = blk.min(axis=1)
     mx = blk.max(axis=1)
@@ -137,9 +143,10 @@ def center(acc, target) -> int:
     return 16 * q - 128
 
 
-def probe_sums(x: np.ndarray, mstart: int, stride: int) -> np.ndarray:
-    """Bytes of the sampled blocks at the 16 bounds range * 2^((mstart + stride k)/64) (k_lfx_probe)."""
-    blk, r, med, rng = _blocks(x)
+def probe_sums(x: np.ndarray, mstart: int, stride: int, off: int = 0) -> np.ndarray:
+    """Bytes of the sampled blocks (sample `off`) at the 16 bounds
+    range * 2^((mstart + stride k)/64) (k_lfx_probe)."""
+    blk, r, med, rng = _blocks(x, off)
     out = np.zeros(16, dtype=np.int64)
     if blk.shape[0] == 0:
         return out
@@ -148,9 +155,10 @@ def probe_sums(x: np.ndarray, mstart: int, stride: int) -> np.ndarray:
     return out
 
 
-def sampled_blocks(x: np.ndarray) -> int:
-    """Every 10th full block of 128 values."""
-    return -(-(x.size // BS) // RATE)
+def sampled_blocks(x: np.ndarray, off: int = 0) -> int:
+    """Every 10th full block of 128 values, from block `off`."""
+    full = x.size // BS
+    return -(-(full - off) // RATE) if full > off else 0
 
 
 def center2(ns, fine, target, mq: int) -> int:
@@ -182,7 +190,7 @@ def features(x: np.ndarray, target: float, mq: int | None = None, mu: int | None
     ultra = probe_sums(x, mu, 1)
     out = np.zeros(F, dtype=np.float64)
     lt = math.log2(float(np.float32(target)))
-    yq, yu = (mq + 128) / 64.0, mu / 64.0
+    yu = mu / 64.0
     kx = (mu - mq) // 16
     u = [(_l2r(b, ns) - lt) if ns > 0 else 0.0 for b in ultra]
     u.append((_l2r(fine[kx + 1], ns) - lt) if (ns > 0 and kx + 1 < 16) else u[15])
@@ -198,10 +206,21 @@ def features(x: np.ndarray, target: float, mq: int | None = None, mu: int | None
                     ys = yu + (j + (-u[j]) / (u[j + 1] - u[j])) / 64.0
                     slope = (u[j + 1] - u[j]) * 64.0
                     break
+    # the second sample's curve at ys, linear between its 1/64 probes
+    ns2 = float(sampled_blocks(x, OFF2))
+    ub = 0.0
+    if ns2 > 0:
+        second = probe_sums(x, mu, 1, OFF2)
+        pos = (ys - yu) * 64.0
+        j0 = 0 if pos <= 0 else (14 if pos >= 15 else int(math.floor(pos)))
+        w = 0.0 if pos <= 0 else (1.0 if pos >= 15 else pos - j0)
+        b0 = _l2r(second[j0], ns2) - lt
+        b1 = _l2r(second[j0 + 1], ns2) - lt
+        ub = b0 + (b1 - b0) * w
     out[0] = lt
     out[1] = ys
     out[2] = min(slope, 256.0)
-    out[3] = yq
+    out[3] = ub
     out[4] = yu
     if ns > 0:
         out[5:13] = [_l2r(fine[4 + k], ns) - lt for k in range(8)]

@@ -1179,6 +1179,133 @@ __device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bo
     store_chunks<T, G>(ob, len, vec, v);
 }
 
+// Consecutive layout: lane sl of the segment decodes the E consecutive values
+// [E*sl, E*sl + E) of the block (chunks NC*sl .. NC*sl + NC-1).  Each value is
+// rebuilt in order with one running word per lane, so inheritance from
+// earlier values of the same lane (szx/src/szxd_float.cc:431-470: the top
+// `lead` bytes come from the predecessor) is resolved as it goes; only the
+// bytes inherited from before the lane's first value are unknown, and one
+// "last writer" scan over the G lane summaries per block supplies them.
+template <typename T, int G, bool FULL>
+__device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob, bool vec, const uint32_t* lut_ld,
+                                                const uint32_t* lut_cm) {
+    using EL = Elem<T>;
+    using U = typename EL::U;
+    constexpr int W = EL::W;
+    constexpr int E = EncCfg<T>::E;
+    constexpr int NC = E / 4;
+    constexpr int TOPSH = 8 * (W - 3);
+    const int sl = (int)(lane_id() & (G - 1));
+    const int reqLength = p[0];
+    const uint32_t mb = ((uint32_t)p[1] << 24) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 8) | p[4];
+    int R, s;
+    split_reqlen(reqLength, &R, &s);
+    R = R < 1 ? 1 : (R > W ? W : R);   // a no-op for valid streams; keeps the shifts defined otherwise
+    const int low = 8 * (W - R);
+    const int Lb = FULL ? G * NC : (len + 3) / 4;
+    const int c0 = sl * NC;            // the lane's first chunk
+    uint32_t ldb[NC], cmb[NC], cnt[NC];
+    uint32_t mine = 0;
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+        const int c = c0 + k;
+        const uint32_t code = (FULL || c < Lb) ? (uint32_t)p[5 + c] : 0u;
+        ldb[k] = lut_ld[code];
+        cmb[k] = lut_cm[code];
+        uint32_t cnt4 = stored_counts(R, ldb[k]);   // max(R - lead, 0) per value
+        if constexpr (!FULL) {
+            const int nin = len - 4 * c;
+            cnt4 &= nin >= 4 ? 0xFFFFFFFFu : (nin <= 0 ? 0u : 0xFFFFFFFFu >> (32 - 8 * nin));
+        }
+        cnt[k] = cnt4;
+        mine += (cnt4 * 0x01010101u) >> 24;
+    }
+    const uint32_t incl = seg_inclusive_sum<G>(mine);
+    const uint32_t ph = (uint32_t)((uintptr_t)p & 15);
+    const uint32_t* buf = (const uint32_t*)(p - ph);
+    uint32_t q = ph + 5 + (uint32_t)Lb + incl - mine;
+    U cur[E];
+    U run = 0;
+    uint32_t mlead = 3;   // smallest lead so far in the lane: its top bytes still come from before the lane
+    uint32_t keep8[NC];   // per value (byte i of chunk k): 8 * bytes inherited from before the lane
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+        const uint32_t ld8 = ldb[k] << 3;
+        uint32_t kb = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t* wp = buf + (q >> 2);
+            const uint32_t w0 = wp[0], w1 = wp[1];
+            const uint32_t inh = top_bytes_mask(byte_of(ld8, i));   // top lead bytes: from the predecessor
+            if constexpr (sizeof(T) == 4) {
+                const uint32_t sp = __funnelshift_r(w0, w1, q << 3) << low;
+                run = (run & inh) | (sp & ~inh);
+            } else {
+                const uint32_t w2 = wp[2];
+                const uint32_t lo = __funnelshift_r(w0, w1, q << 3), hi = __funnelshift_r(w1, w2, q << 3);
+                const unsigned long long sp = (((unsigned long long)hi << 32) | lo) << low;
+                const unsigned long long ih = (unsigned long long)inh << 32;
+                run = (run & ih) | (sp & ~ih);
+            }
+            cur[4 * k + i] = run;
+            const uint32_t cm = byte_of(cmb[k], i);
+            mlead = cm < mlead ? cm : mlead;
+            kb |= mlead << (8 * i);
+            q += byte_of(cnt[k], i);
+        }
+        keep8[k] = kb << 3;
+    }
+    // lane summary: [25:24] smallest lead in the lane, [23:0] top three bytes of its last value
+    uint32_t inc = (mlead << 24) | ((uint32_t)(run >> TOPSH) & 0xFFFFFFu);
+#pragma unroll
+    for (int d = 1; d < G; d <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xffffffffu, inc, d, G);
+        if (sl >= d) inc = lw_op(o, inc);
+    }
+    uint32_t ex = __shfl_up_sync(0xffffffffu, inc, 1, G);
+    if (sl == 0) ex = kLwNone;
+    const uint32_t carry = (ex & 0xFFFFFFu) << 8;   // top three bytes of a 32-bit word
+    const T med = widen_median<T>(__uint_as_float(mb));
+    T v[E];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t keep = top_bytes_mask(byte_of(keep8[k], i));
+            U u = cur[4 * k + i];
+            if constexpr (sizeof(T) == 4) u |= carry & keep;
+            else u |= (unsigned long long)(carry & keep) << 32;
+            u <<= s;
+            cur[4 * k + i] = u;
+            v[4 * k + i] = EL::add(EL::of(u), med);
+            bad |= v[4 * k + i] != v[4 * k + i];
+        }
+    }
+    if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = xadd(EL::of(cur[e]), med);
+    }
+    // store the lane's E consecutive values (a segment called with len 0 --
+    // a constant block, whose median is already stored -- stores nothing)
+    const int f0 = E * sl;
+    if (vec && f0 + E <= len) {
+#pragma unroll
+        for (int k = 0; k < NC; k++) {
+            if constexpr (sizeof(T) == 4) {
+                *(float4*)(ob + f0 + 4 * k) = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+            } else {
+                *(double2*)(ob + f0 + 4 * k) = make_double2(v[4 * k], v[4 * k + 1]);
+                *(double2*)(ob + f0 + 4 * k + 2) = make_double2(v[4 * k + 2], v[4 * k + 3]);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; e++)
+            if (f0 + e < len) ob[f0 + e] = v[e];
+    }
+}
+
 // ------------------------------------------------------------------ decode, pipelined tiles
 //
 // One producer warp per CTA walks the CTA's tiles ahead of the decoders: it
@@ -1435,9 +1562,9 @@ __global__ void __launch_bounds__(kDecThreadsP, kDecCtasPerSm) k_blocked_decode(
         const uint8_t* stage = dsm + slot * TL::kStage;
         // the whole warp takes one path: segments that decode nothing store nothing either way
         if (__all_sync(0xffffffffu, !coded || blen == TL::kBsMax))
-            dec_segment<T, G, true>(stage + (coded ? info : 0u), coded ? blen : 0, ob, vec, lut_ld, lut_cm);
+            dec_segment_seq<T, G, true>(stage + (coded ? info : 0u), coded ? blen : 0, ob, vec, lut_ld, lut_cm);
         else
-            dec_segment<T, G, false>(stage + (coded ? info : 0u), coded ? blen : 0, ob, vec, lut_ld, lut_cm);
+            dec_segment_seq<T, G, false>(stage + (coded ? info : 0u), coded ? blen : 0, ob, vec, lut_ld, lut_cm);
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[slot]);
     }

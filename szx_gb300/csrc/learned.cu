@@ -19,7 +19,7 @@
 //   0       log2(target)
 //   1       ys: where the sampled ratio curve crosses the target (finest level)
 //   2       the curve's slope there, d log2(ratio) / d y
-//   3       yq: centre of the quarter-step window
+//   3       the second sample's curve at ys, relative to the target (see below)
 //   4       yu: start of the 1/64-step window
 //   5..12   quarter-step curve at y = yq - 1 .. yq + 0.75, relative to the target
 //   13..28  1/64-step curve at y = yu + j/64, j = 0..15, relative to the target
@@ -32,7 +32,12 @@
 // found in three passes, 16 probes each: y = -1.5j per field over every 4th
 // sampled block (coarse), then per row a window of quarter steps around the
 // coarse crossing, then 1/64 steps across the quarter step that brackets the
-// target.  Every probe bound is range * 2^(m/64) for an integer m, rounded
+// target.  A second, disjoint sample -- every 10th full block from block 5
+// on -- is evaluated at the same 1/64 probes; its curve at ys (interpolated)
+// tells how far the first sample's crossing is off from what a twice larger
+// sample sees: information the first sample's curve does not hold, which
+// lets the network predict part of the sampling miss.
+// Every probe bound is range * 2^(m/64) for an integer m, rounded
 // the same way everywhere, and all sums are integers (deterministic atomics).
 // A non-constant block's bytes change only where the bound crosses a power of
 // two, so the curve is a staircase with smooth parts from the constant
@@ -73,7 +78,8 @@ constexpr int kTileBlocks = 32;     // sampled blocks per warp tile
 constexpr int kCoarseStep = 4;      // the coarse curve uses every 4th sampled block (every 40th block)
 constexpr int kAcc = 18;            // per field, over the coarse blocks: count, bytes[16], radius-0 blocks
 constexpr int A_NS = 0, A_BYTES = 1, A_ZERO = 17;
-constexpr int kRowAcc = 32;         // per row: quarter-step bytes[16], 1/64-step bytes[16]
+constexpr int kRowAcc = 48;         // per row: quarter-step bytes[16], 1/64-step bytes[16], second sample's [16]
+constexpr int kOff2 = 5;            // the second sample: blocks 5, 15, 25, ...
 constexpr int kQMin = -100, kQMax = 4;   // quarter-step window centre, quarters of y
 constexpr double kBracketStop = 1.0 / 1024;   // searches stop on a measured bracket this narrow
 
@@ -92,6 +98,7 @@ __constant__ float c_frac64[64];       // 2^(i / 64), rounded to float
 struct LfxField {
     const float* x;
     unsigned long long n, ns, tile0;   // values, sampled blocks, first launch-wide tile
+    unsigned long long ns2;            // blocks of the second sample (<= ns)
 };
 
 struct LfxWork {
@@ -191,8 +198,8 @@ __device__ __forceinline__ float lfx_range_of(const uint32_t* mm, int f) {
 // Values 4*lane .. 4*lane+3 of sampled block k (128 values) and the block's
 // radius and median as the codec computes them.
 __device__ __forceinline__ void lfx_block(const float* x, unsigned long long k, int lane, float v[4], float* r,
-                                          float* med) {
-    const float* p = x + k * kRate * 128 + 4 * lane;
+                                          float* med, int off = 0) {
+    const float* p = x + (k * kRate + off) * 128 + 4 * lane;
     if (((uintptr_t)x & 15) == 0) {
         const float4 q = *(const float4*)p;
         v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
@@ -370,7 +377,8 @@ __global__ void k_lfx_center2(const LfxField* F, const unsigned long long* racc,
 // items (row, tile of the row's field).
 __global__ void __launch_bounds__(256) k_lfx_probe(const LfxField* F, const uint32_t* mm, int nrows, const int* rows,
                                                    const int* mstart, int stride, const unsigned long long* rtile0,
-                                                   unsigned long long items, unsigned long long* racc, int slot) {
+                                                   unsigned long long items, unsigned long long* racc, int slot,
+                                                   int off) {
     const int lane = threadIdx.x & 31;
     const unsigned long long w0 = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nw = (gridDim.x * (unsigned long long)blockDim.x) >> 5;
@@ -386,11 +394,12 @@ __global__ void __launch_bounds__(256) k_lfx_probe(const LfxField* F, const uint
         uint32_t bytes[kFine];
 #pragma unroll
         for (int k = 0; k < kFine; k++) bytes[k] = 0;
+        // the second sample's blocks are tiled like the first's (ns2 <= ns)
         const unsigned long long k0 = (g - rtile0[r]) * kTileBlocks;
-        const unsigned long long k1 = min(k0 + kTileBlocks, D.ns);
+        const unsigned long long k1 = min(k0 + kTileBlocks, off ? D.ns2 : D.ns);
         for (unsigned long long k = k0; k < k1; k++) {
             float v[4], rr, med;
-            lfx_block(D.x, k, lane, v, &rr, &med);
+            lfx_block(D.x, k, lane, v, &rr, &med, off);
             lfx_block_bytes<kFine>(v, rr, med, eb, bytes, lane);
         }
         unsigned long long* a = racc + (size_t)r * kRowAcc + slot;
@@ -436,7 +445,20 @@ __global__ void k_lfx_rows(const LfxField* F, const unsigned long long* acc, con
     x[0] = (float)lt;
     x[1] = (float)ys;
     x[2] = (float)fmin(slope, 256.0);
-    x[3] = (float)yq;
+    // the second sample's curve at ys: linear between its 1/64 probes (held
+    // at the window's ends outside it)
+    double ub = 0.0;
+    const double ns2 = (double)F[f].ns2;
+    if (ns2 > 0) {
+        const double pos = (ys - yu) * 64.0;
+        const int j0 = pos <= 0 ? 0 : (pos >= kFine - 1 ? kFine - 2 : (int)floor(pos));
+        const double w = pos <= 0 ? 0.0 : (pos >= kFine - 1 ? 1.0 : pos - j0);
+        const double b0 = lfx_log2_ratio((double)ra[2 * kFine + j0], ns2) - lt;
+        const double b1 = lfx_log2_ratio((double)ra[2 * kFine + j0 + 1], ns2) - lt;
+        ub = b0 + (b1 - b0) * w;
+    }
+    (void)yq;
+    x[3] = (float)ub;
     x[4] = (float)yu;
     for (int k = 0; k < 8; k++) x[5 + k] = ns > 0 ? (float)(lfx_log2_ratio((double)ra[4 + k], ns) - lt) : 0.f;
     for (int j = 0; j < kFine; j++) x[13 + j] = (float)u[j];
@@ -938,6 +960,8 @@ cudaError_t lfx_prepare(SZxG_Batch* b, size_t rows) {
         L.n = F.n;
         const unsigned long long full = F.n / 128;
         L.ns = (full + kRate - 1) / kRate;
+        L.ns2 = (full + kRate - 1 - kOff2) / kRate;   // blocks kOff2, kOff2 + 10, ... below full
+        if (full <= (unsigned long long)kOff2) L.ns2 = 0;
         L.tile0 = t;
         w->ftiles[f] = (L.ns + kTileBlocks - 1) / kTileBlocks;
         t += w->ftiles[f];
@@ -1036,13 +1060,15 @@ cudaError_t lfx_rows(SZxG_Batch* b, int nrows, const int* h_rows, const float* h
     if (items) {
         TraceScope tr("lfx_probe", s);
         k_lfx_probe<<<lfx_grid(items), 256, 0, s>>>(w->d_f, w->mm, nrows, w->rows, w->mq, 16, w->rtile0, items,
-                                                    w->racc, 0);
+                                                    w->racc, 0, 0);
     }
     k_lfx_center2<<<rg, 128, 0, s>>>(w->d_f, w->racc, nrows, w->rows, w->tgt, w->mq, w->mu);
     if (items) {
         TraceScope tr("lfx_probe", s);
         k_lfx_probe<<<lfx_grid(items), 256, 0, s>>>(w->d_f, w->mm, nrows, w->rows, w->mu, 1, w->rtile0, items,
-                                                    w->racc, kFine);
+                                                    w->racc, kFine, 0);
+        k_lfx_probe<<<lfx_grid(items), 256, 0, s>>>(w->d_f, w->mm, nrows, w->rows, w->mu, 1, w->rtile0, items,
+                                                    w->racc, 2 * kFine, kOff2);
     }
     const int n = std::max(nrows, b->nf);
     k_lfx_rows<<<(n + 127) / 128, 128, 0, s>>>(w->d_f, w->acc, w->mm, nrows, w->rows, w->tgt, w->mq, w->mu, w->racc,
