@@ -1186,8 +1186,23 @@ __device__ __forceinline__ void dec_segment(const uint8_t* p, int len, T* ob, bo
 // `lead` bytes come from the predecessor) is resolved as it goes; only the
 // bytes inherited from before the lane's first value are unknown, and one
 // "last writer" scan over the G lane summaries per block supplies them.
+// 32-byte stores (sm_100 and later): a lane's 8 floats / 4 doubles at a
+// 32-byte aligned address, so that lanes writing consecutive 64-byte runs fill
+// whole 32-byte sectors.
+__device__ __forceinline__ void st_v8(float* p, const float* v) {
+    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0]), "f"(v[1]), "f"(v[2]),
+                 "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+                 : "memory");
+}
+__device__ __forceinline__ void st_v8(double* p, const double* v) {
+    asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(p), "d"(v[0]), "d"(v[1]), "d"(v[2]), "d"(v[3])
+                 : "memory");
+}
+
+// vec: 0 scalar stores, 1 16-byte stores, 2 32-byte stores (the output's
+// alignment and the block's byte size allow them).
 template <typename T, int G, bool FULL>
-__device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob, bool vec, const uint32_t* lut_ld,
+__device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob, int vec, const uint32_t* lut_ld,
                                                 const uint32_t* lut_cm) {
     using EL = Elem<T>;
     using U = typename EL::U;
@@ -1289,7 +1304,11 @@ __device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob
     // store the lane's E consecutive values (a segment called with len 0 --
     // a constant block, whose median is already stored -- stores nothing)
     const int f0 = E * sl;
-    if (vec && f0 + E <= len) {
+    constexpr int V8 = 32 / (int)sizeof(T);   // values per 32-byte store
+    if (vec == 2 && f0 + E <= len) {
+#pragma unroll
+        for (int k = 0; k < E / V8; k++) st_v8(ob + f0 + V8 * k, v + V8 * k);
+    } else if (vec && f0 + E <= len) {
 #pragma unroll
         for (int k = 0; k < NC; k++) {
             if constexpr (sizeof(T) == 4) {
@@ -1522,7 +1541,11 @@ __global__ void __launch_bounds__(kDecThreadsP, kDecCtasPerSm) k_blocked_decode(
 
     // -------------------------------------------------------------- consumers
     T* out = (T*)a.out;
-    bool vec = ((bs * (int)sizeof(T)) & 15) == 0 && ((uintptr_t)out & 15) == 0;
+    auto vec_of = [&](const T* o) {
+        const uintptr_t al = (uintptr_t)o | (uintptr_t)(bs * (int)sizeof(T));
+        return (al & 31) == 0 ? 2 : ((al & 15) == 0 ? 1 : 0);
+    };
+    int vec = vec_of(out);
     unsigned long long n = h.n;
     const int seg = lane / G;
     const int lb = warp * TL::kBpw + seg;
@@ -1539,7 +1562,7 @@ __global__ void __launch_bounds__(kDecThreadsP, kDecCtasPerSm) k_blocked_decode(
             out = (T*)D->out;
             n = D->n;
             lt = t - (long long)D->dec_tile0;
-            vec = ((bs * (int)sizeof(T)) & 15) == 0 && ((uintptr_t)out & 15) == 0;
+            vec = vec_of(out);
         }
         const unsigned long long b = (unsigned long long)lt * TB + lb;
         const int kind = s_kind[slot][lb];

@@ -692,4 +692,10 @@ __device__ __forceinline__ unsigned long long prefix_resolve_win(unsigned long l
     return pa;
 }
 
+// 16-byte asynchronous global -> shared copies (cp.async, the LSU path: they
+// do not queue behind the TMA unit's bulk copies), L2 only.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 }  // namespace szxg
