@@ -274,6 +274,7 @@ struct EncTile {
     static constexpr int kDynSmem = 4 * kBuf;
     static_assert(kGroups <= 8 && kBlocks % kBpw == 0, "one block group per warp");
     static_assert(kBlocks <= 64, "a tile's sizes are scanned as two warp-wide halves");
+    static_assert(kBlocks * kMaxPay < 65535, "a tile's byte count + 1 fits the 16-bit aggregate words");
     static_assert(kIn % 16 == 0 && kBuf % 16 == 0, "TMA destinations stay 16-byte aligned");
 };
 
@@ -302,8 +303,10 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
     constexpr int NGRP = TB / BPW;
     extern __shared__ __align__(128) uint8_t dsm[];
     __shared__ unsigned long long bar[4];
-    __shared__ __align__(16) unsigned long long s_lbw[kLbWin];   // look-back window (status words)
-    __shared__ unsigned long long bar_lb;
+    __shared__ __align__(16) uint16_t s_w16[2][kLbWin + 8];   // look-back windows (16-bit aggregates)
+    __shared__ long long s_an_t, s_wlo[2];                     // placement anchor tile; window first tiles
+    __shared__ unsigned long long s_an_incl;                   // the anchor's inclusive prefix
+    __shared__ int s_an_f, s_wok[2];                           // its field; window states
     __shared__ uint32_t s_size[4][TB], s_med[4][TB];
     __shared__ uint8_t s_state[4][TB];
     __shared__ uint32_t s_agg[4];
@@ -322,7 +325,6 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
     auto buf_ptr = [&](int r) { return dsm + r * TL::kBuf; };
     if (threadIdx.x == 0) {
         for (int r = 0; r < 4; r++) mbar_init(&bar[r], 1);
-        mbar_init(&bar_lb, 1);
         mbar_fence_init();
         for (int r = 0; r < 2; r++) {
             s_tile[r] = (long long)atomicAdd(a.tile_ctr, 1ull);
@@ -372,30 +374,48 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
     };
 
     unsigned long long nnc_cta = 0;   // warp 0 lane 0, single field: non-constant blocks of this CTA's tiles
-    // thread 0: copy the status words of tile t's predecessors [lo, t) (at most
-    // kLbWin, the nearest ones) to shared memory; returns lo
-    uint32_t lb_phase = 0;
-    auto window_load = [&](const BlkField* F, long long t) -> long long {
-        if (t <= 0) return 0;
-        long long lo = t > kLbWin ? t - kLbWin : 0;
-        lo = (lo + 1) & ~1ll;                                           // 16-byte aligned source
-        const uint32_t bytes = (uint32_t)(((t - lo + 1) & ~1ll) * 8);   // whole 16-byte units, within st
-        if (threadIdx.x == 0) {
-            fence_proxy_async();   // the window's last reads and this CTA's publications come first
-            mbar_arrive_expect_tx(&bar_lb, bytes);
-            tma_load_1d(s_lbw, FV(F, st_enc) + lo, bytes, &bar_lb);
-        }
-        return lo;
+    // Placement (warp 0).  A tile's offset is the inclusive prefix of this
+    // CTA's previous tile (the anchor, known here) plus the aggregates of the
+    // tiles claimed between the two, read from the field's 16-bit aggregate
+    // words: a window of at most kLbWin of them is copied into shared memory
+    // an iteration before it is needed.  No anchor in the same field within
+    // kLbWin tiles, or an aggregate not yet published, falls back to the
+    // global look-back over the 64-bit status words.
+    // (the anchor and window state live in shared memory: warp 0 alone uses
+    // them, lane 0 writes, and registers stay free for the statistics)
+    if (threadIdx.x == 0) {
+        s_an_t = -1;
+        s_an_f = -1;
+        s_an_incl = 0;
+    }
+    auto agg16_of = [&](const BlkField* F) {
+        return (uint16_t*)(FV(F, st_enc) + enc_tile_words(FV(F, nb)));
     };
-    // warp 0: offset of tile t of field F (metadata set r), its sizes / medians / state bits by block
-    auto resolve = [&](const BlkField* F, long long t, int r, long long lo) {
-        const uint32_t agg = s_agg[r];
-        unsigned long long base = 0;
-        if (t > 0) {
-            if (!mbar_wait(&bar_lb, lb_phase) && lane == 0) atomicExch(a.err, kErrLookback);
-            lb_phase ^= 1u;
-            base = prefix_resolve_win(FV(F, st_enc), t, agg, a.err, s_lbw, lo);
+    auto win_issue = [&](const BlkField* F, int f, long long t, int buf) {
+        int ok = 0;
+        long long lo = 0;
+        const long long an_t = s_an_t;
+        if (t > 0 && an_t >= 0 && s_an_f == f && an_t < t && t - an_t - 1 <= kLbWin) {
+            if (t - an_t == 1) {
+                ok = 2;
+            } else {
+                lo = (an_t + 1) & ~7ll;
+                const int units = (int)((t - lo + 7) >> 3);
+                const uint16_t* src = agg16_of(F) + lo;
+                for (int u = lane; u < units; u += 32) cp_async16(&s_w16[buf][8 * u], src + 8 * u);
+                ok = 1;
+            }
         }
+        if (lane == 0) {
+            s_wlo[buf] = lo;
+            s_wok[buf] = ok;
+        }
+        __syncwarp();
+    };
+    // warp 0: tile t of field F (metadata set r) placed at `base`: its sizes /
+    // medians / state bits by block, the capacity check, the field's totals
+    auto meta = [&](const BlkField* F, long long t, int r, unsigned long long base) {
+        const uint32_t agg = s_agg[r];
         const bool cap_ok = base + agg <= FV(F, payload_cap);
         const unsigned long long tb0 = (unsigned long long)t * TB;
         uint32_t m01[2];
@@ -425,6 +445,45 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
             s_skip = !cap_ok;
         }
     };
+    // warp 0: place tile t of field f (metadata set r; its window in buffer buf)
+    auto place = [&](const BlkField* F, int f, long long t, int r, int buf) {
+        const uint32_t agg = s_agg[r];
+        unsigned long long base = 0;
+        if (t > 0) {
+            const int ok = s_wok[buf];
+            const long long lo = s_wlo[buf];
+            const long long an_t = s_an_t;
+            const unsigned long long an_incl = s_an_incl;
+            bool placed = false;
+            if (ok == 2) {
+                base = an_incl;
+                placed = true;
+            } else if (ok == 1) {
+                cp_async_wait_all();
+                __syncwarp();
+                unsigned long long sum = 0;
+                bool ready = true;
+                for (long long i = an_t + 1 + lane; i < t; i += 32) {
+                    const uint32_t v = s_w16[buf][i - lo];
+                    ready = ready && v != 0;
+                    sum += v - 1;
+                }
+                if (__all_sync(0xffffffffu, ready)) {
+                    base = an_incl + warp_sum(sum);
+                    placed = true;
+                }
+            }
+            if (!placed) base = prefix_resolve(FV(F, st_enc), t, agg, a.err);   // publishes t's inclusive prefix
+            else if (lane == 0) st_volatile64(&FV(F, st_enc)[t], kS64Inc | ((base + agg) & kS64Val));
+        }
+        meta(F, t, r, base);
+        if (lane == 0) {
+            s_an_t = t;
+            s_an_f = f;
+            s_an_incl = base + agg;
+        }
+        __syncwarp();
+    };
     auto copy_out = [&](const BlkField* F, int r) {
         if (!s_skip) cta_copy_realign(buf_ptr(r), s_agg[r], FV(F, payload) + s_base);
     };
@@ -435,7 +494,6 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
     int eb_f = -1, eb_exp = 0;    // field whose bound is loaded, the bound's exponent
     float eb = 0.f;
     int f1 = 0, f2 = 0;
-    long long lo1 = 0;            // window base of T_{j-1}
     int j = 0;
     for (;; j++) {
         const int r = j & 3;
@@ -445,7 +503,7 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
             const long long gn = s_tile[rn];
             if (gn < nt) issue(gn, s_fld[rn], rn);
         }
-        if (warp == 0 && t2 >= 0) resolve(fld(f2), t2, (j - 2) & 3, lo1);
+        if (warp == 0 && t2 >= 0) place(fld(f2), f2, t2, (j - 2) & 3, (j - 1) & 1);
         const long long g = s_tile[r];
         if (g >= nt) break;
         const int f = s_fld[r];
@@ -485,7 +543,7 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
         }
         __syncthreads();   // statistics in (T_j's input is dead), T_{j-2} placed
         // warp 0: T_{j-1}'s look-back window, in flight until the next iteration
-        if (warp == 0 && t1 >= 0) lo1 = window_load(fld(f1), t1);
+        if (warp == 0 && t1 >= 0) win_issue(fld(f1), f1, t1, j & 1);
         // every warp: the tile's block offsets (two warp-wide halves)
         const bool in0 = lane < TB;
         const uint32_t sz0 = in0 ? s_size[r][lane] : 0;
@@ -500,7 +558,10 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
         }
         if (warp == 0) {
             const uint32_t agg = __shfl_sync(0xffffffffu, i1, 31);
-            if (lane == 0) s_agg[r] = agg;
+            if (lane == 0) {
+                s_agg[r] = agg;
+                st_relaxed16(agg16_of(F) + t, agg + 1);
+            }
             prefix_publish(FV(F, st_enc), t, agg);
         }
         if (mine && b.state == 1) {
@@ -515,16 +576,16 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
         f1 = f;
     }
     // this CTA's last two tiles: T_{j-2} was placed at the top of the final
-    // iteration, T_{j-1} still needs its look-back
+    // iteration, T_{j-1} still needs its window and placement
     if (t2 >= 0) {
         __syncthreads();
         copy_out(fld(f2), (j - 2) & 3);
     }
     if (t1 >= 0) {
-        __syncthreads();   // the window buffer and s_base are free again
+        __syncthreads();   // s_base is free again
         if (warp == 0) {
-            const long long lo = window_load(fld(f1), t1);
-            resolve(fld(f1), t1, (j - 1) & 3, lo);
+            win_issue(fld(f1), f1, t1, j & 1);
+            place(fld(f1), f1, t1, (j - 1) & 3, j & 1);
         }
         __syncthreads();
         copy_out(fld(f1), (j - 1) & 3);

@@ -135,7 +135,12 @@ constexpr size_t kWsHeaderClear = 512;
 // on 32-byte boundaries: the look-back reads them with 16-byte vector loads.
 constexpr size_t kAsmBlocksPerTile = 2048;
 constexpr size_t round4(size_t w) { return (w + 3) & ~size_t(3); }
-constexpr size_t enc_status_words(size_t nb) { return round4(nb / 8 + 9); }
+// The encoder's region: its 64-bit words, then (at enc_tile_words) one 16-bit
+// word per tile, aggregate + 1 (0: not published), with room for the
+// 16-byte reads past the last tile.
+constexpr size_t enc_tile_words(size_t nb) { return round4(nb / 8 + 9); }
+constexpr size_t enc_agg16_words(size_t nb) { return round4((nb / 8 + 40) / 4); }
+constexpr size_t enc_status_words(size_t nb) { return enc_tile_words(nb) + enc_agg16_words(nb); }
 constexpr size_t blocked_status_words(size_t nb) { return enc_status_words(nb) + round4(nb / kAsmBlocksPerTile + 9); }
 
 // Host: fault in the pages of a fresh malloc'd output buffer [p, p+n) on a
