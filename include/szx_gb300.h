@@ -217,6 +217,29 @@ int SZxG_batch_run(SZxG_Batch* batch, SZxG_StreamInfo* d_info, void* stream);
 int SZxG_batch_status(SZxG_Batch* batch, void* stream);
 void SZxG_batch_destroy(SZxG_Batch* batch);
 
+/* Launch shapes by field-size class (no counterpart in the reference).  A
+ * batch groups its fields by size class -- the first entry whose maxValues is
+ * >= the field's value count, the last entry for larger fields -- and codes
+ * each class with one persistent launch per kernel of that class's shape:
+ * encoder tile variant (0: 16 KiB of input per tile, 8 warps per CTA; 1:
+ * 8 KiB, 4 warps -- float blocks of 65..128 values only, else as 0) and CTAs
+ * per SM of the encoder and the decoder (0: as many as fit).  Shapes change
+ * how the work is cut, never a stream.  The table in effect is read from the
+ * autotuner's file (tuning/batch_shapes.txt beside the library, or the file
+ * the SZXG_TUNING_FILE environment variable names); without one, a single
+ * class with the default shape.  At most 8 entries, maxValues ascending;
+ * n == 0 reloads the file.  Applies to batches created afterwards. */
+typedef struct {
+    unsigned long long maxValues;
+    int encTileVariant;
+    int encCtasPerSm;
+    int decCtasPerSm;
+    int reserved;
+} SZxG_LaunchShape;
+int SZxG_set_launch_shapes(const SZxG_LaunchShape* table, int n);
+/* The table in effect (up to cap entries into table); returns its length. */
+int SZxG_get_launch_shapes(SZxG_LaunchShape* table, int cap);
+
 /* Change the bounds of a compress plan's fields and which fields a run codes:
  * fieldIndex[k] (k < nActive) in that order, all fields when fieldIndex is
  * NULL (nActive == nFields); absErrBound[k] is field fieldIndex[k]'s new bound

@@ -1,21 +1,35 @@
-// Batches: many fields of one type and block size coded by one persistent
-// launch per kernel over a device work queue of (field, block-range) tiles.
+// Batches: many fields of one type and block size coded by persistent
+// launches over a device work queue of (field, block-range) tiles.
 // Compress (direction 0): fastMode 2, 3, 4.  Decompress (direction 1):
 // fastMode 3 and 4, whose size index makes every stream's payload offsets a
 // scan; a fastMode-2 stream needs the single-stream boundary search.
 //
 // The blocked kernels take a table of fields (a single-field call is a table
-// of one): a launch-wide tile index maps to (field, local tile) by a binary
-// search over the fields' first tiles, and every field keeps its own
-// look-back status words, totals, scratch and stream.  Tiles are handed out
-// in field order from one atomic counter, so a field's tiles are always
-// acquired before any later field's, which is all the per-field look-back
-// needs to make progress.  This file plans a batch (layout of the per-field
-// scratch in one allocation, the field table on the device) and runs it as a
+// of one): a launch-wide tile index maps to (field, local tile) through a
+// tile map, and every field keeps its own look-back status words, totals,
+// scratch and stream.  Tiles are handed out in field order from one atomic
+// counter, so a field's tiles are always acquired before any later field's,
+// which is all the per-field look-back needs to make progress.
+//
+// Fields are grouped by size class (a table of value-count bounds, each with
+// its launch shape: encoder tile size and CTAs per SM of the encoder and the
+// decoder), and each class is one persistent launch per kernel with its own
+// shape.  The table comes from the tuning file written by the project's
+// autotuner (szx_gb300/tune.py: tuning/batch_shapes.txt next to the
+// library, or the file SZXG_TUNING_FILE names), or from
+// SZxG_set_launch_shapes; with neither, one class with the default shape.
+// The shape never changes a stream: only how the work is cut and spread.
+//
+// This file plans a batch (layout of the per-field scratch in one
+// allocation, the field table and tile map on the device) and runs it as a
 // handful of memsets and launches that a CUDA graph can capture.
+#include <dlfcn.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "../../include/szx_gb300.h"
@@ -32,38 +46,165 @@ SZxG_Batch* fail(int code) {
     return nullptr;
 }
 
+// ------------------------------------------------------------------ launch shapes by size class
+
+struct ShapeEntry {
+    unsigned long long max_values;
+    LaunchShape shape;
+};
+std::mutex g_shape_mu;
+std::vector<ShapeEntry> g_shapes;   // ascending max_values; the last one takes every larger field
+bool g_shapes_loaded = false;
+
+std::string tuning_path() {
+    if (const char* e = getenv("SZXG_TUNING_FILE")) return e;
+    Dl_info info;
+    if (dladdr((void*)&tuning_path, &info) && info.dli_fname) {
+        std::string so = info.dli_fname;
+        const size_t k = so.find_last_of('/');
+        return (k == std::string::npos ? std::string(".") : so.substr(0, k)) + "/tuning/batch_shapes.txt";
+    }
+    return "";
+}
+
+// "max_values enc_tile_variant enc_ctas_per_sm dec_ctas_per_sm" per line, '#' comments
+std::vector<ShapeEntry> read_tuning(const std::string& path) {
+    std::vector<ShapeEntry> v;
+    FILE* f = path.empty() ? nullptr : fopen(path.c_str(), "r");
+    if (!f) return v;
+    char line[256];
+    while (fgets(line, sizeof line, f)) {
+        if (line[0] == '#') continue;
+        unsigned long long m = 0;
+        int tv = 0, ec = 0, dc = 0;
+        if (sscanf(line, "%llu %d %d %d", &m, &tv, &ec, &dc) != 4) continue;
+        if ((int)v.size() == kMaxBatchParts || (!v.empty() && m <= v.back().max_values)) break;
+        LaunchShape s;
+        s.enc_tile_variant = tv == 1 ? 1 : 0;
+        s.enc_ctas_per_sm = ec < 0 ? 0 : ec;
+        s.dec_ctas_per_sm = dc < 0 ? 0 : dc;
+        v.push_back({m, s});
+    }
+    fclose(f);
+    return v;
+}
+
+void ensure_shapes_locked() {
+    if (g_shapes_loaded) return;
+    g_shapes = read_tuning(tuning_path());
+    if (g_shapes.empty()) g_shapes.push_back({~0ull, LaunchShape{}});
+    g_shapes_loaded = true;
+}
+
 }  // namespace
 
+int batch_class_of(unsigned long long n, int* nclasses) {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    ensure_shapes_locked();
+    if (nclasses) *nclasses = (int)g_shapes.size();
+    for (size_t k = 0; k < g_shapes.size(); k++)
+        if (n <= g_shapes[k].max_values) return (int)k;
+    return (int)g_shapes.size() - 1;
+}
+
+LaunchShape batch_class_shape(int k) {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    ensure_shapes_locked();
+    return g_shapes[(size_t)k < g_shapes.size() ? (size_t)k : g_shapes.size() - 1].shape;
+}
+
+// The fields a compress run codes, grouped by class in a stable order, their
+// device table and tile map (per class: tiles numbered from 0, field
+// indices relative to the class's first table entry).
 cudaError_t batch_select(SZxG_Batch* b, int nActive, const int* h_idx, const float* h_eb, cudaStream_t s) {
     if (b->direction != 0 || nActive < 1 || nActive > b->nf) return cudaErrorInvalidValue;
     if (!h_idx && nActive != b->nf) return cudaErrorInvalidValue;
-    const size_t tb = (size_t)blocked_tile_blocks(b->dtype, b->bs);
-    std::vector<BlkField> run((size_t)nActive);
-    unsigned long long et = 0, at = 0;
+    const int ncls = (int)b->class_shape.size();
+    std::vector<std::vector<int>> by(ncls);
     for (int k = 0; k < nActive; k++) {
         const int f = h_idx ? h_idx[k] : k;
         if (f < 0 || f >= b->nf) return cudaErrorInvalidValue;
         if (h_eb) b->tab[f].eb = h_eb[k];
-        BlkField F = b->tab[f];
-        F.enc_tiles = (F.nb + tb - 1) / tb; F.enc_tile0 = et; et += F.enc_tiles;
-        F.asm_tiles = (F.nb + kAsmBlocksPerTile - 1) / kAsmBlocksPerTile; F.asm_tile0 = at; at += F.asm_tiles;
-        run[(size_t)k] = F;
+        by[b->cls[f]].push_back(f);
     }
-    b->enc_total = et;
-    b->asm_total = at;
-    b->one = run[0];
-    b->nrun = nActive;
+    b->run.clear();
+    b->parts.clear();
+    b->h_tile_field.clear();
+    for (int c = 0; c < ncls; c++) {
+        if (by[c].empty()) continue;
+        BatchPart P;
+        P.shape = b->class_shape[c];
+        P.i0 = (int)b->run.size();
+        P.map0 = b->h_tile_field.size();
+        unsigned long long et = 0, at = 0;
+        for (int f : by[c]) {
+            BlkField F = b->tab[f];   // enc_tiles already for this class's tile size
+            F.enc_tile0 = et; et += F.enc_tiles;
+            F.asm_tile0 = at; at += F.asm_tiles;
+            for (unsigned long long t = 0; t < F.enc_tiles; t++)
+                b->h_tile_field.push_back((uint32_t)(b->run.size() - P.i0));
+            b->run.push_back(F);
+        }
+        P.i1 = (int)b->run.size();
+        P.enc_total = et;
+        P.asm_total = at;
+        b->parts.push_back(P);
+    }
     // pageable sources: each copy is staged before the call returns, ordered after earlier runs on s
-    cudaError_t e = cudaMemcpyAsync(b->d_fields, run.data(), sizeof(BlkField) * (size_t)nActive,
+    cudaError_t e = cudaMemcpyAsync(b->d_fields, b->run.data(), sizeof(BlkField) * b->run.size(),
                                     cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess || nActive == 1) return e;
-    b->h_tile_field.resize(et);
-    for (int k = 0; k < nActive; k++)
-        for (unsigned long long t = 0; t < run[(size_t)k].enc_tiles; t++) b->h_tile_field[run[(size_t)k].enc_tile0 + t] = (uint32_t)k;
-    return cudaMemcpyAsync(b->d_tile_field, b->h_tile_field.data(), 4 * et, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_tile_field, b->h_tile_field.data(), 4 * b->h_tile_field.size(),
+                            cudaMemcpyHostToDevice, s);
+    return e;
 }
 
 extern "C" {
+
+int SZxG_set_launch_shapes(const SZxG_LaunchShape* table, int n) {
+    if (n < 0 || n > kMaxBatchParts || (n > 0 && !table)) {
+        set_last_error(SZXG_ERR_ARG);
+        return SZXG_ERR_ARG;
+    }
+    std::vector<ShapeEntry> v;
+    for (int k = 0; k < n; k++) {
+        const SZxG_LaunchShape& t = table[k];
+        if ((k > 0 && t.maxValues <= table[k - 1].maxValues) || (t.encTileVariant != 0 && t.encTileVariant != 1) ||
+            t.encCtasPerSm < 0 || t.decCtasPerSm < 0) {
+            set_last_error(SZXG_ERR_ARG);
+            return SZXG_ERR_ARG;
+        }
+        LaunchShape s;
+        s.enc_tile_variant = t.encTileVariant;
+        s.enc_ctas_per_sm = t.encCtasPerSm;
+        s.dec_ctas_per_sm = t.decCtasPerSm;
+        v.push_back({t.maxValues, s});
+    }
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    if (n == 0) {
+        g_shapes_loaded = false;
+        ensure_shapes_locked();
+    } else {
+        g_shapes = v;
+        g_shapes_loaded = true;
+    }
+    set_last_error(SZXG_OK);
+    return SZXG_OK;
+}
+
+int SZxG_get_launch_shapes(SZxG_LaunchShape* table, int cap) {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    ensure_shapes_locked();
+    const int n = (int)g_shapes.size();
+    for (int k = 0; k < n && k < cap && table; k++) {
+        table[k].maxValues = g_shapes[k].max_values;
+        table[k].encTileVariant = g_shapes[k].shape.enc_tile_variant;
+        table[k].encCtasPerSm = g_shapes[k].shape.enc_ctas_per_sm;
+        table[k].decCtasPerSm = g_shapes[k].shape.dec_ctas_per_sm;
+        table[k].reserved = 0;
+    }
+    return n;
+}
 
 int SZxG_batch_set_bounds(SZxG_Batch* b, int nActive, const int* fieldIndex, const float* absErrBound, void* stream) {
     if (!b || b->direction != 0) { set_last_error(SZXG_ERR_ARG); return SZXG_ERR_ARG; }
@@ -79,11 +220,21 @@ static SZxG_Batch* create_decode(int fastMode, int dataType, int blockSize, int 
     if (blockSize < 1 || blockSize > 256) return fail(SZXG_ERR_ARG);
     const size_t nf = (size_t)nFields, es = dataType == 0 ? 4 : 8;
     const size_t tb = (size_t)blocked_dec_tile_blocks(dataType, blockSize);
-    // layout: table | results | counters+err | headers | zeroed (errors, look-back words) | offsets, ranks
+    // fields by class, in a stable order: the device table's order
+    int ncls = 1;
+    std::vector<std::vector<size_t>> by;
+    for (size_t f = 0; f < nf; f++) {
+        const int c = batch_class_of(fields[f].nbEle, &ncls);
+        if (by.size() < (size_t)ncls) by.resize((size_t)ncls);
+        by[(size_t)c].push_back(f);
+    }
+    std::vector<size_t> order;
+    for (auto& v : by) order.insert(order.end(), v.begin(), v.end());
+    // layout: table | results | counters+err | headers | tile map | zeroed (errors, look-back words) | offsets, ranks
     size_t off = 0;
     const size_t o_tab = off; off += a256(sizeof(DecField) * nf);
     const size_t o_res = off; off += a256(sizeof(StreamResult) * nf);
-    const size_t o_ctr = off; off += 256;
+    const size_t o_ctr = off; off += 512;
     const size_t o_hdr = off; off += a256(sizeof(BlockedHdr) * nf);
     unsigned long long dec_tiles_all = 0;
     for (size_t f = 0; f < nf; f++) dec_tiles_all += ((fields[f].nbEle + blockSize - 1) / blockSize + tb - 1) / tb;
@@ -116,39 +267,49 @@ static SZxG_Batch* create_decode(int fastMode, int dataType, int blockSize, int 
     uint8_t* base = (uint8_t*)b->dev;
     b->results = (StreamResult*)(base + o_res);
     b->counters = (unsigned long long*)(base + o_ctr);
-    b->err = (int*)(base + o_ctr + 64);
+    b->err = (int*)(base + o_ctr + 384);
     b->zero = base + o_zero;
     b->zero_bytes = zero_bytes;
     std::vector<DecField> tab(nf);
-    unsigned long long it = 0, dt = 0;
-    for (size_t f = 0; f < nf; f++) {
-        const SZxG_Field& S = fields[f];
-        DecField& D = tab[f];
-        memset(&D, 0, sizeof D);
-        D.s = (const uint8_t*)S.in; D.len = S.inBytes; D.n = S.nbEle;
-        D.nb = (S.nbEle + blockSize - 1) / blockSize;
-        D.out = S.out;
-        D.hdr = (BlockedHdr*)(base + o_hdr) + f;
-        D.P = (unsigned long long*)(base + o_p[f]);
-        D.RW = (uint32_t*)(base + o_rw[f]);
-        unsigned long long* st = (unsigned long long*)(base + o_st[f]);
-        for (int k = 0; k < 3; k++) D.stA[k] = st + k * ta[f];
-        st += 3 * ta[f];
-        for (int k = 0; k < 3; k++) D.stB[k] = st + k * tbw[f];
-        D.idxA_tiles = ta[f]; D.idxB_tiles = tbw[f];
-        D.idx_tile0 = it; it += ta[f] + tbw[f];
-        D.dec_tiles = (D.nb + tb - 1) / tb;
-        D.dec_tile0 = dt; dt += D.dec_tiles;
-        D.err = (int*)(base + o_err) + f;
+    for (size_t c = 0, k = 0; c < by.size(); c++) {
+        if (by[c].empty()) continue;
+        BatchPart P;
+        P.shape = batch_class_shape((int)c);
+        P.i0 = (int)k;
+        P.map0 = b->h_tile_field.size();
+        unsigned long long it = 0, dt = 0;
+        for (size_t f : by[c]) {
+            const SZxG_Field& S = fields[f];
+            DecField& D = tab[k];
+            memset(&D, 0, sizeof D);
+            D.s = (const uint8_t*)S.in; D.len = S.inBytes; D.n = S.nbEle;
+            D.nb = (S.nbEle + blockSize - 1) / blockSize;
+            D.out = S.out;
+            D.hdr = (BlockedHdr*)(base + o_hdr) + f;
+            D.P = (unsigned long long*)(base + o_p[f]);
+            D.RW = (uint32_t*)(base + o_rw[f]);
+            unsigned long long* st = (unsigned long long*)(base + o_st[f]);
+            for (int q = 0; q < 3; q++) D.stA[q] = st + q * ta[f];
+            st += 3 * ta[f];
+            for (int q = 0; q < 3; q++) D.stB[q] = st + q * tbw[f];
+            D.idxA_tiles = ta[f]; D.idxB_tiles = tbw[f];
+            D.idx_tile0 = it; it += ta[f] + tbw[f];
+            D.dec_tiles = (D.nb + tb - 1) / tb;
+            D.dec_tile0 = dt; dt += D.dec_tiles;
+            D.err = (int*)(base + o_err) + f;
+            D.res = b->results + f;
+            for (unsigned long long t = 0; t < D.dec_tiles; t++) b->h_tile_field.push_back((uint32_t)(k - P.i0));
+            k++;
+        }
+        P.i1 = (int)k;
+        P.idx_total = it;
+        P.dec_total = dt;
+        b->parts.push_back(P);
     }
-    b->idx_total = it;
-    b->dec_total = dt;
     b->d_dec = (DecField*)(base + o_tab);
     b->d_tile_field = (uint32_t*)(base + o_map);
-    b->h_tile_field.resize(dt);
-    for (size_t f = 0; f < nf; f++)
-        for (unsigned long long t = 0; t < tab[f].dec_tiles; t++) b->h_tile_field[tab[f].dec_tile0 + t] = (uint32_t)f;
-    if (cudaMemcpy(b->d_tile_field, b->h_tile_field.data(), 4 * dt, cudaMemcpyHostToDevice) != cudaSuccess ||
+    if (cudaMemcpy(b->d_tile_field, b->h_tile_field.data(), 4 * b->h_tile_field.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
         cudaMemcpy(b->d_dec, tab.data(), sizeof(DecField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(b->dev);
@@ -168,16 +329,25 @@ SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blo
         return fail(SZXG_ERR_UNSUPPORTED);
     if (blockSize < 1 || blockSize > 256 || (fastMode == kBlocked && blockSize > 255)) return fail(SZXG_ERR_ARG);
     const size_t nf = (size_t)nFields;
-    const size_t tb = (size_t)blocked_tile_blocks(dataType, blockSize);
     const size_t hdr = fastMode == kBlocked ? 13 : 20;
-    // layout: table | results | counters+err | zeroed status words and totals | scratch
+    // every field's class; the class's tile size sets the field's tile count
+    std::vector<int> cls(nf);
+    int ncls = 1;
+    for (size_t f = 0; f < nf; f++) cls[f] = batch_class_of(fields[f].nbEle, &ncls);
+    std::vector<LaunchShape> cshape((size_t)ncls);
+    std::vector<size_t> ctb((size_t)ncls);
+    for (int c = 0; c < ncls; c++) {
+        cshape[(size_t)c] = batch_class_shape(c);
+        ctb[(size_t)c] = (size_t)blocked_tile_blocks(dataType, blockSize, cshape[(size_t)c].enc_tile_variant);
+    }
+    // layout: table | results | counters+err | tile map | zeroed status words and totals | scratch
     size_t off = 0;
     const size_t o_tab = off; off += a256(sizeof(BlkField) * nf);
     const size_t o_res = off; off += a256(sizeof(StreamResult) * nf);
-    const size_t o_ctr = off; off += 256;
+    const size_t o_ctr = off; off += 512;
     unsigned long long tiles_all = 0;
     for (size_t f = 0; f < nf; f++)
-        tiles_all += ((fields[f].nbEle + blockSize - 1) / blockSize + tb - 1) / tb;
+        tiles_all += ((fields[f].nbEle + blockSize - 1) / blockSize + ctb[(size_t)cls[f]] - 1) / ctb[(size_t)cls[f]];
     const size_t o_map = off; off += a256(4 * tiles_all);
     const size_t o_zero = off;
     std::vector<size_t> o_st(nf), o_tot(nf), o_sz(nf), o_md(nf), o_ss(nf);
@@ -207,20 +377,20 @@ SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blo
     uint8_t* base = (uint8_t*)b->dev;
     b->results = (StreamResult*)(base + o_res);
     b->counters = (unsigned long long*)(base + o_ctr);
-    b->err = (int*)(base + o_ctr + 64);
+    b->err = (int*)(base + o_ctr + 384);
     b->zero = base + o_zero;
     b->zero_bytes = zero_bytes;
-    std::vector<BlkField> tab(nf);
-    unsigned long long et = 0, at = 0;
+    b->tab.resize(nf);
     for (size_t f = 0; f < nf; f++) {
         const SZxG_Field& S = fields[f];
         const size_t nb = (S.nbEle + blockSize - 1) / blockSize, sb = (nb + 7) / 8;
         const size_t qfix = hdr + sb + 4 * nb;
-        BlkField& F = tab[f];
+        const size_t tb = ctb[(size_t)cls[f]];
+        BlkField& F = b->tab[f];
         memset(&F, 0, sizeof F);
         F.x = S.in; F.n = S.nbEle; F.nb = nb;
-        F.enc_tiles = (nb + tb - 1) / tb; F.enc_tile0 = et; et += F.enc_tiles;
-        F.asm_tiles = (nb + kAsmBlocksPerTile - 1) / kAsmBlocksPerTile; F.asm_tile0 = at; at += F.asm_tiles;
+        F.enc_tiles = (nb + tb - 1) / tb;
+        F.asm_tiles = (nb + kAsmBlocksPerTile - 1) / kAsmBlocksPerTile;
         F.eb = S.absErrBound;
         F.params = nullptr;
         F.out = (uint8_t*)S.out;
@@ -234,18 +404,11 @@ SZxG_Batch* SZxG_batch_create(int direction, int fastMode, int dataType, int blo
         F.tot = (Totals*)(base + o_tot[f]);
         F.res = b->results + f;
     }
-    b->enc_total = et;
-    b->asm_total = at;
-    b->one = tab[0];
-    b->tab = tab;
-    b->nrun = nFields;
+    b->cls = cls;
+    b->class_shape = cshape;
     b->d_fields = (BlkField*)(base + o_tab);
     b->d_tile_field = (uint32_t*)(base + o_map);
-    b->h_tile_field.resize(et);
-    for (size_t f = 0; f < nf; f++)
-        for (unsigned long long t = 0; t < tab[f].enc_tiles; t++) b->h_tile_field[tab[f].enc_tile0 + t] = (uint32_t)f;
-    if (cudaMemcpy(b->d_tile_field, b->h_tile_field.data(), 4 * et, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(b->d_fields, tab.data(), sizeof(BlkField) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (batch_select(b, nFields, nullptr, nullptr, 0) != cudaSuccess || cudaStreamSynchronize(0) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(b->dev);
         delete b;
@@ -259,14 +422,20 @@ int SZxG_batch_run(SZxG_Batch* b, SZxG_StreamInfo* d_info, void* stream) {
     if (!b) { set_last_error(SZXG_ERR_ARG); return SZXG_ERR_ARG; }
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemsetAsync(b->zero, 0, b->zero_bytes, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->counters, 0, 128, s);
-    if (e == cudaSuccess && b->direction == 1)
-        e = launch_blocked_decode_fields(b->mode, b->dtype, b->bs, b->nf, b->d_dec, b->d_tile_field, b->idx_total,
-                                         b->dec_total,
-                                         b->counters, b->results, b->err, s);
-    else if (e == cudaSuccess)
-        e = launch_blocked_encode_fields(b->mode, b->dtype, b->bs, b->nrun, b->one, b->nrun > 1 ? b->d_fields : nullptr,
-                                         b->d_tile_field, b->enc_total, b->asm_total, b->counters, b->err, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->counters, 0, 32 * kMaxBatchParts, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->err, 0, sizeof(int), s);
+    for (size_t k = 0; k < b->parts.size() && e == cudaSuccess; k++) {
+        const BatchPart& P = b->parts[k];
+        const int n = P.i1 - P.i0;
+        unsigned long long* ctr = b->counters + 4 * k;
+        if (b->direction == 1)
+            e = launch_blocked_decode_fields(b->mode, b->dtype, b->bs, n, b->d_dec + P.i0, b->d_tile_field + P.map0,
+                                             P.idx_total, P.dec_total, ctr, b->results, b->err, s, P.shape);
+        else
+            e = launch_blocked_encode_fields(b->mode, b->dtype, b->bs, n, b->run[(size_t)P.i0],
+                                             n > 1 ? b->d_fields + P.i0 : nullptr, b->d_tile_field + P.map0,
+                                             P.enc_total, P.asm_total, ctr, b->err, s, P.shape);
+    }
     if (e == cudaSuccess && d_info)
         e = cudaMemcpyAsync(d_info, b->results, sizeof(StreamResult) * b->nf, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) {

@@ -41,6 +41,7 @@ namespace szxg {
 // save.
 constexpr int kEncTileBytes = 16384;
 constexpr int kEncWarpsPerSm = 24;
+constexpr int kWinRepolls = 32;   // window re-reads before the global look-back walk
 constexpr int kIdxThreads = 256;
 constexpr int kIdxItems = 8;   // items per thread in the index scans
 
@@ -254,12 +255,12 @@ __device__ __forceinline__ void cta_copy_realign(const uint8_t* stg, uint32_t n,
     }
 }
 
-template <typename T, int G>
+template <typename T, int G, int TBYTES = kEncTileBytes>
 struct EncTile {
     static constexpr int E = EncCfg<T>::E;
     static constexpr int kBsMax = G * E;                               // largest block of this variant
     static constexpr int kBpw = 32 / G;                                // blocks per warp
-    static constexpr int kRaw = kEncTileBytes / (kBsMax * (int)sizeof(T));
+    static constexpr int kRaw = TBYTES / (kBsMax * (int)sizeof(T));
     static constexpr int kBlocks = kRaw >= 64 ? 64 : (kRaw < 8 ? 8 : kRaw);   // blocks per tile
     static constexpr int kGroups = kBlocks / kBpw;                     // warps with blocks
     static constexpr int kWarps = kGroups > 4 ? kGroups : 4;
@@ -295,9 +296,10 @@ struct EncTile {
 // CTA's own previous tile (already placed); otherwise it falls back to the
 // global walk.  A segment of G lanes owns one block from its statistics to
 // its emission.
-template <typename T, int G, bool MULTI>
-__global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCtas) k_blocked_encode(EncArgs a) {
-    using TL = EncTile<T, G>;
+template <typename T, int G, bool MULTI, int TBYTES = kEncTileBytes>
+__global__ void __launch_bounds__(EncTile<T, G, TBYTES>::kThreads, EncTile<T, G, TBYTES>::kMinCtas)
+    k_blocked_encode(EncArgs a) {
+    using TL = EncTile<T, G, TBYTES>;
     constexpr int TB = TL::kBlocks;
     constexpr int BPW = TL::kBpw;
     constexpr int NGRP = TB / BPW;
@@ -459,18 +461,28 @@ __global__ void __launch_bounds__(EncTile<T, G>::kThreads, EncTile<T, G>::kMinCt
                 base = an_incl;
                 placed = true;
             } else if (ok == 1) {
-                cp_async_wait_all();
-                __syncwarp();
-                unsigned long long sum = 0;
-                bool ready = true;
-                for (long long i = an_t + 1 + lane; i < t; i += 32) {
-                    const uint32_t v = s_w16[buf][i - lo];
-                    ready = ready && v != 0;
-                    sum += v - 1;
-                }
-                if (__all_sync(0xffffffffu, ready)) {
-                    base = an_incl + warp_sum(sum);
-                    placed = true;
+                // a window with aggregates not yet published is copied again
+                // (one round trip each) a few times before the global walk
+                const int units = (int)((t - lo + 7) >> 3);
+                for (int attempt = 0;; attempt++) {
+                    cp_async_wait_all();
+                    __syncwarp();
+                    unsigned long long sum = 0;
+                    bool ready = true;
+                    for (long long i = an_t + 1 + lane; i < t; i += 32) {
+                        const uint32_t v = s_w16[buf][i - lo];
+                        ready = ready && v != 0;
+                        sum += v - 1;
+                    }
+                    if (__all_sync(0xffffffffu, ready)) {
+                        base = an_incl + warp_sum(sum);
+                        placed = true;
+                        break;
+                    }
+                    if (attempt == kWinRepolls) break;
+                    __nanosleep(128);
+                    const uint16_t* src = agg16_of(F) + lo;
+                    for (int u = lane; u < units; u += 32) cp_async16(&s_w16[buf][8 * u], src + 8 * u);
                 }
             }
             if (!placed) base = prefix_resolve(FV(F, st_enc), t, agg, a.err);   // publishes t's inclusive prefix
@@ -760,9 +772,10 @@ size_t blocked_bound(int layout, int dtype, size_t n, int bs) {
     return hdr + sb + 4 * nb + nb * (5 + ((size_t)bs + 3) / 4) + es * n + 64;
 }
 
-template <typename T, int G>
-static cudaError_t run_encode(EncArgs a, cudaStream_t s) {
-    using TL = EncTile<T, G>;
+// ctas_per_sm: 0 as many as fit, else at most that many.
+template <typename T, int G, int TBYTES = kEncTileBytes>
+static cudaError_t run_encode(EncArgs a, int ctas_per_sm, cudaStream_t s) {
+    using TL = EncTile<T, G, TBYTES>;
     static bool attr_set[64] = {false};
     static int per_sm[64] = {0};
     int dev = 0;
@@ -771,26 +784,31 @@ static cudaError_t run_encode(EncArgs a, cudaStream_t s) {
     if (!attr_set[dev]) {
         // the ring needs the largest shared-memory carveout for 3 CTAs per SM
         cudaError_t e = cudaSuccess;
-        for (auto k : {k_blocked_encode<T, G, false>, k_blocked_encode<T, G, true>}) {
+        for (auto k : {k_blocked_encode<T, G, false, TBYTES>, k_blocked_encode<T, G, true, TBYTES>}) {
             if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TL::kDynSmem);
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         }
         int occ = 0;
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_blocked_encode<T, G, false>, TL::kThreads,
-                                                              TL::kDynSmem);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_blocked_encode<T, G, false, TBYTES>,
+                                                              TL::kThreads, TL::kDynSmem);
         if (e != cudaSuccess) return e;
         per_sm[dev] = occ < 1 ? 1 : occ;
         attr_set[dev] = true;
     }
-    const size_t g = (size_t)sm_count() * per_sm[dev];
+    const int cps = ctas_per_sm > 0 && ctas_per_sm < per_sm[dev] ? ctas_per_sm : per_sm[dev];
+    const size_t g = (size_t)sm_count() * cps;
     const int grid = (int)(a.total_tiles < g ? a.total_tiles : g);
     TraceScope tr("blocked_encode", s);
-    if (a.nf > 1) k_blocked_encode<T, G, true><<<grid, TL::kThreads, TL::kDynSmem, s>>>(a);
-    else k_blocked_encode<T, G, false><<<grid, TL::kThreads, TL::kDynSmem, s>>>(a);
+    if (a.nf > 1) k_blocked_encode<T, G, true, TBYTES><<<grid, TL::kThreads, TL::kDynSmem, s>>>(a);
+    else k_blocked_encode<T, G, false, TBYTES><<<grid, TL::kThreads, TL::kDynSmem, s>>>(a);
     return cudaGetLastError();
 }
+// The one encoder tile variant a launch shape can pick besides the default:
+// 8 KiB tiles (16 blocks, 4 warps, 6 CTAs per SM) for float blocks of 65..128
+// values.
+constexpr int kEncTileBytesSmall = 8192;
 
 static int lanes_for_bs(int dtype, int bs) {
     const int per = dtype == 0 ? 16 : 8;   // values per lane
@@ -798,8 +816,9 @@ static int lanes_for_bs(int dtype, int bs) {
     return need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
 }
 
-int blocked_tile_blocks(int dtype, int bs) {
+int blocked_tile_blocks(int dtype, int bs, int tile_variant) {
     const int G = lanes_for_bs(dtype, bs);
+    if (tile_variant == 1 && dtype == 0 && G == 8) return EncTile<float, 8, kEncTileBytesSmall>::kBlocks;
     if (dtype == 0) {
         switch (G) {
             case 1: return EncTile<float, 1>::kBlocks;
@@ -822,7 +841,8 @@ int blocked_tile_blocks(int dtype, int bs) {
 cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, const BlkField& one,
                                          const BlkField* d_fields, const uint32_t* d_tile_field,
                                          unsigned long long enc_total, unsigned long long asm_total,
-                                         unsigned long long* counters, int* err, cudaStream_t s) {
+                                         unsigned long long* counters, int* err, cudaStream_t s,
+                                         const LaunchShape& shape) {
     if (nf < 1 || enc_total == 0 || (nf > 1 && !d_tile_field)) return cudaErrorInvalidValue;
     EncArgs a;
     a.one = one;
@@ -838,20 +858,24 @@ cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, 
     const int G = lanes_for_bs(dtype, bs);
     if (dtype == 0) {
         switch (G) {
-            case 1: e = run_encode<float, 1>(a, s); break;
-            case 2: e = run_encode<float, 2>(a, s); break;
-            case 4: e = run_encode<float, 4>(a, s); break;
-            case 8: e = run_encode<float, 8>(a, s); break;
-            default: e = run_encode<float, 16>(a, s); break;
+            case 1: e = run_encode<float, 1>(a, shape.enc_ctas_per_sm, s); break;
+            case 2: e = run_encode<float, 2>(a, shape.enc_ctas_per_sm, s); break;
+            case 4: e = run_encode<float, 4>(a, shape.enc_ctas_per_sm, s); break;
+            case 8:
+                e = shape.enc_tile_variant == 1
+                        ? run_encode<float, 8, kEncTileBytesSmall>(a, shape.enc_ctas_per_sm, s)
+                        : run_encode<float, 8>(a, shape.enc_ctas_per_sm, s);
+                break;
+            default: e = run_encode<float, 16>(a, shape.enc_ctas_per_sm, s); break;
         }
     } else {
         switch (G) {
-            case 1: e = run_encode<double, 1>(a, s); break;
-            case 2: e = run_encode<double, 2>(a, s); break;
-            case 4: e = run_encode<double, 4>(a, s); break;
-            case 8: e = run_encode<double, 8>(a, s); break;
-            case 16: e = run_encode<double, 16>(a, s); break;
-            default: e = run_encode<double, 32>(a, s); break;
+            case 1: e = run_encode<double, 1>(a, shape.enc_ctas_per_sm, s); break;
+            case 2: e = run_encode<double, 2>(a, shape.enc_ctas_per_sm, s); break;
+            case 4: e = run_encode<double, 4>(a, shape.enc_ctas_per_sm, s); break;
+            case 8: e = run_encode<double, 8>(a, shape.enc_ctas_per_sm, s); break;
+            case 16: e = run_encode<double, 16>(a, shape.enc_ctas_per_sm, s); break;
+            default: e = run_encode<double, 32>(a, shape.enc_ctas_per_sm, s); break;
         }
     }
     if (e != cudaSuccess) return e;
@@ -883,7 +907,7 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
     // status words of both look-backs, then totals / result / error / counters
     if ((e = cudaMemsetAsync(ws.st_word, 0, 8 * blocked_status_words(nb), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync((uint8_t*)ws.totals, 0, kWsHeaderClear, s)) != cudaSuccess) return e;
-    const size_t tb = (size_t)blocked_tile_blocks(dtype, bs);
+    const size_t tb = (size_t)blocked_tile_blocks(dtype, bs, 0);
     BlkField F;
     F.x = x; F.n = n; F.nb = nb;
     F.enc_tiles = (nb + tb - 1) / tb; F.enc_tile0 = 0;
@@ -899,7 +923,7 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
     F.tot = ws.totals;
     F.res = ws.result;
     return launch_blocked_encode_fields(layout, dtype, bs, 1, F, nullptr, nullptr, F.enc_tiles, F.asm_tiles,
-                                        ws.counters, ws.err, s);
+                                        ws.counters, ws.err, s, LaunchShape{});
 }
 
 // ------------------------------------------------------------------ decode
@@ -1687,11 +1711,12 @@ static cudaError_t run_decode(const uint8_t* s, size_t len, size_t nb, const Wor
 
 template <typename T, int G>
 static cudaError_t run_decode_fields(const DecField* F, const uint32_t* tf, int nf, int bs, unsigned long long total,
-                                     int native, int* lerr, cudaStream_t st) {
+                                     int native, int* lerr, int ctas_per_sm, cudaStream_t st) {
     using TL = DecTileV<T, G>;
     cudaError_t e = dec_attr<T, G, true>();
     if (e != cudaSuccess) return e;
-    const size_t cap = (size_t)sm_count() * kDecCtasPerSm;
+    const int cps = ctas_per_sm > 0 && ctas_per_sm < kDecCtasPerSm ? ctas_per_sm : kDecCtasPerSm;
+    const size_t cap = (size_t)sm_count() * cps;
     const int grid = (int)(total < cap ? (total ? total : 1) : cap);
     DecArgs a = {};
     a.native_medians = native; a.err = lerr;
@@ -1724,7 +1749,7 @@ __global__ void k_blocked_decode_finish(const DecField* F, int nf, int esize, St
     r.nb_const = D.hdr->ok ? D.hdr->nc : 0;
     r.eb = 0.f;
     r.status = st;
-    res[f] = r;
+    *(D.res ? D.res : res + f) = r;
     if (st) atomicCAS(err, 0, st);
 }
 
@@ -1732,7 +1757,7 @@ cudaError_t launch_blocked_decode_fields(int layout, int dtype, int bs, int nf, 
                                          const uint32_t* d_tile_field, unsigned long long idx_total,
                                          unsigned long long dec_total,
                                          unsigned long long* counters, StreamResult* res, int* err,
-                                         cudaStream_t s) {
+                                         cudaStream_t s, const LaunchShape& shape) {
     if (layout != kRandomAccess && layout != kRandomAccessNative) return cudaErrorInvalidValue;
     if (bs < 1 || bs > 256 || nf < 1) return cudaErrorInvalidValue;
     int* lerr = (int*)(counters + 3);
@@ -1750,20 +1775,20 @@ cudaError_t launch_blocked_decode_fields(int layout, int dtype, int bs, int nf, 
     cudaError_t e;
     if (dtype == 0) {
         switch (dec_lanes(dtype, bs)) {
-            case 1: e = run_decode_fields<float, 1>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            case 2: e = run_decode_fields<float, 2>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            case 4: e = run_decode_fields<float, 4>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            case 8: e = run_decode_fields<float, 8>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            default: e = run_decode_fields<float, 16>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 1: e = run_decode_fields<float, 1>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            case 2: e = run_decode_fields<float, 2>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            case 4: e = run_decode_fields<float, 4>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            case 8: e = run_decode_fields<float, 8>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            default: e = run_decode_fields<float, 16>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
         }
     } else {
         switch (dec_lanes(dtype, bs)) {
-            case 1: e = run_decode_fields<double, 1>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            case 2: e = run_decode_fields<double, 2>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            case 4: e = run_decode_fields<double, 4>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            case 8: e = run_decode_fields<double, 8>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            case 16: e = run_decode_fields<double, 16>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
-            default: e = run_decode_fields<double, 32>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, s); break;
+            case 1: e = run_decode_fields<double, 1>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            case 2: e = run_decode_fields<double, 2>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            case 4: e = run_decode_fields<double, 4>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            case 8: e = run_decode_fields<double, 8>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            case 16: e = run_decode_fields<double, 16>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
+            default: e = run_decode_fields<double, 32>(d_fields, d_tile_field, nf, bs, dec_total, native, lerr, shape.dec_ctas_per_sm, s); break;
         }
     }
     if (e != cudaSuccess) return e;

@@ -94,6 +94,7 @@ struct DecField {
     unsigned long long dec_tile0, dec_tiles;     // launch-wide first decode tile, decode tiles
     int* err;                                    // this stream's error word, zeroed
     int pad;
+    StreamResult* res;                           // where its outcome goes (NULL: res[f] of the launch)
 };
 
 // ------------------------------------------------------------------ workspace
@@ -209,11 +210,21 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
 // with d_tile_field[g] = the field of launch-wide encode tile g;
 // counters[0..2] and err zeroed by the caller, like every field's status
 // words and totals.
-int blocked_tile_blocks(int dtype, int bs);
+// Launch shape of the blocked kernels (chosen per field-size class for
+// batches): the encoder's tile variant (0: 16 KiB of input, 1: 8 KiB -- float
+// blocks of 65..128 values only, else the default) and CTAs per SM of the
+// encoder and the decoder (0: as many as fit).
+struct LaunchShape {
+    int enc_tile_variant = 0;
+    int enc_ctas_per_sm = 0;
+    int dec_ctas_per_sm = 0;
+};
+int blocked_tile_blocks(int dtype, int bs, int tile_variant = 0);
 cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, const BlkField& one,
                                          const BlkField* d_fields, const uint32_t* d_tile_field,
                                          unsigned long long enc_total, unsigned long long asm_total,
-                                         unsigned long long* counters, int* err, cudaStream_t s);
+                                         unsigned long long* counters, int* err, cudaStream_t s,
+                                         const LaunchShape& shape = LaunchShape{});
 // Blocked decode of nf streams (layouts 3, 4) in one launch per kernel: the
 // headers are parsed into the fields' hdr, counters[0] and every field's
 // look-back words and error word zeroed by the caller; res[f] receives field
@@ -226,7 +237,7 @@ cudaError_t launch_blocked_decode_fields(int layout, int dtype, int bs, int nf, 
                                          const uint32_t* d_tile_field, unsigned long long idx_total,
                                          unsigned long long dec_total,
                                          unsigned long long* counters, StreamResult* res, int* err,
-                                         cudaStream_t s);
+                                         cudaStream_t s, const LaunchShape& shape = LaunchShape{});
 // Blocked decode (layouts 3, 4).
 cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream, size_t len, size_t n, int bs,
                                   void* d_out, const Workspace& ws, cudaStream_t s);

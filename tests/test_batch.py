@@ -270,3 +270,36 @@ def test_batch_streams_and_decodes_match_the_oracle(env, mode, dtname, bs):
     for k, xh in enumerate(hosts):
         z = O.decompress(mode, xh.dtype, got[k], xh.size)
         assert np.array_equal(outs[k].cpu().numpy().view(it), z.view(it)), (k, xh.size)
+
+
+def test_every_launch_shape_gives_the_same_streams(env):
+    """Fields grouped by size class, each class one persistent launch with its
+    own shape (encoder tile size and threads per CTA, CTAs per SM of encoder
+    and decoder): for every shape the tuner may choose, and for a table that
+    splits the fields into three classes, every stream equals the single-field
+    stream and every batched decode equals the single-field decode."""
+    from szx_gb300 import tune
+    torch = env[0]
+    rng = np.random.default_rng(31)
+    sizes = [1, 129, 4097, 65536] + [int(v) for v in np.exp(rng.uniform(np.log(1 << 12), np.log(1 << 21), 20))]
+    xs, ebs = _fields(torch, torch.float32, sizes, 37)
+    want = [_single(env, 3, x, 128, eb) for x, eb in zip(xs, ebs)]
+    want_dec = None
+    M = (1 << 64) - 1
+    tables = [[(M, tv, ec, dc)] for tv, ec in tune.ENC_CANDIDATES for dc in tune.DEC_CANDIDATES[:2]]
+    tables.append([(1 << 14, 1, 4, 2), (1 << 18, 0, 2, 3), (M, 1, 0, 0)])
+    try:
+        for table in tables:
+            tune.set_shapes(table)
+            assert tune.get_shapes() == table
+            got = _batch(env, 3, xs, 128, ebs)
+            assert got == want, table
+            streams = [torch.tensor(np.frombuffer(s, np.uint8).copy(), device="cuda") for s in got]
+            outs, infos, st = _batch_decompress(env, 3, streams, sizes, 128, torch.float32)
+            assert st == 0 and all(i.status == 0 for i in infos), table
+            if want_dec is None:
+                want_dec = [_single_decompress(env, 3, s, n, 128, torch.float32) for s, n in zip(streams, sizes)]
+            for k in range(len(sizes)):
+                assert _same(outs[k], want_dec[k]), (table, k)
+    finally:
+        tune.set_shapes([])
