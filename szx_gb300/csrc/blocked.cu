@@ -1330,8 +1330,14 @@ __device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob
     uint32_t keep8[NC];   // per value (byte i of chunk k): 8 * bytes inherited from before the lane
 #pragma unroll
     for (int k = 0; k < NC; k++) {
+        // byte-wise min(running minimum within the chunk, minimum before it):
+        // all values are <= 3, so bit 7 of a byte of (c | 0x80..) - m says c >= m
+        const uint32_t M = mlead * 0x01010101u;
+        const uint32_t ge = (((cmb[k] | 0x80808080u) - M) & 0x80808080u) >> 7;
+        const uint32_t kb = (M & (ge * 0xFFu)) | (cmb[k] & ~(ge * 0xFFu));
+        keep8[k] = kb << 3;
+        mlead = kb >> 24;
         const uint32_t ld8 = ldb[k] << 3;
-        uint32_t kb = 0;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const uint32_t* wp = buf + (q >> 2);
@@ -1348,12 +1354,8 @@ __device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob
                 run = (run & ih) | (sp & ~ih);
             }
             cur[4 * k + i] = run;
-            const uint32_t cm = byte_of(cmb[k], i);
-            mlead = cm < mlead ? cm : mlead;
-            kb |= mlead << (8 * i);
             q += byte_of(cnt[k], i);
         }
-        keep8[k] = kb << 3;
     }
     // lane summary: [25:24] smallest lead in the lane, [23:0] top three bytes of its last value
     uint32_t inc = (mlead << 24) | ((uint32_t)(run >> TOPSH) & 0xFFFFFFu);
@@ -1367,7 +1369,6 @@ __device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob
     const uint32_t carry = (ex & 0xFFFFFFu) << 8;   // top three bytes of a 32-bit word
     const T med = widen_median<T>(__uint_as_float(mb));
     T v[E];
-    bool bad = false;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
 #pragma unroll
@@ -1379,8 +1380,20 @@ __device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob
             u <<= s;
             cur[4 * k + i] = u;
             v[4 * k + i] = EL::add(EL::of(u), med);
-            bad |= v[4 * k + i] != v[4 * k + i];
         }
+    }
+    // a NaN result anywhere (three-input max with NaN propagation, float)
+    bool bad;
+    if constexpr (sizeof(T) == 4) {
+        float hn = v[0];
+#pragma unroll
+        for (int e = 1; e + 1 < E; e += 2) hn = fmax3_nan(hn, v[e], v[e + 1]);
+        hn = fmax_nan(hn, v[E - 1]);
+        bad = hn != hn;
+    } else {
+        bad = false;
+#pragma unroll
+        for (int e = 0; e < E; e++) bad |= v[e] != v[e];
     }
     if (__any_sync(0xffffffffu, bad)) {
 #pragma unroll
