@@ -681,6 +681,25 @@ def run_batched(args, wl, fields=None):
         dper = [evs[k].elapsed_time(evs[k + 1]) for k in range(nf)]
     dloop = statistics.median(dloop)
     dpf = np.array(dper)
+    # the launch shapes the autotuner chose per size class against the fixed
+    # default shape, same fields, median of graph replays each
+    from szx_gb300 import tune
+    del ys
+    torch.cuda.empty_cache()
+    tuned_table = tune.get_shapes()
+    t_ms = tune.time_batch(xs, ebs, outs, mode, bs)
+    tune.set_shapes([((1 << 64) - 1, 0, 0, 0)])
+    try:
+        f_ms = tune.time_batch(xs, ebs, outs, mode, bs)
+    finally:
+        tune.set_shapes([])
+    shapes = {"table": [list(e) for e in tuned_table],
+              "tuned_compress_gbs": round(total_in / (t_ms[0] / 1000) / 1e9, 2),
+              "tuned_decompress_gbs": round(total_in / (t_ms[1] / 1000) / 1e9, 2),
+              "fixed_compress_gbs": round(total_in / (f_ms[0] / 1000) / 1e9, 2),
+              "fixed_decompress_gbs": round(total_in / (f_ms[1] / 1000) / 1e9, 2),
+              "note": "table: per size class (max values, encoder tile variant, encoder CTAs/SM, decoder CTAs/SM; "
+                      "0 = as many as fit); fixed: one class, default shape"}
     line = {
         "metric": "batched compress GB/s (mixed float32 fields, ABS)", "value": round(total_in / (batched_ms / 1000) / 1e9, 2),
         "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(batched_ms, 4),
@@ -694,6 +713,7 @@ def run_batched(args, wl, fields=None):
                                "p99_ms": round(float(np.percentile(pf, 99)), 4)},
         "single_field_gbs": round(big_gbs, 2), "single_field_elements": xs[big].numel(),
         "batched_vs_single": round(total_in / (batched_ms / 1000) / 1e9 / big_gbs, 3),
+        "launch_shapes": shapes,
         "decompress": {"batched_gbs": round(total_in / (dec_ms / 1000) / 1e9, 2), "ms_per_step": round(dec_ms, 4),
                        "per_field_gbs": round(total_in / (dloop / 1000) / 1e9, 2),
                        "p50_ms": round(float(np.percentile(dpf, 50)), 4),
