@@ -7,7 +7,9 @@
  *   non-constant block: median (native float), reqLength u8, 2-bit lead
  *   codes (blockSize / 4 bytes), mid bytes.
  *
- * Per block (szx/src/cuszx_float.cu:221-300, 118-219): min / max, radius =
+ * Per block (szx/src/cuszx_float.cu:221-300, 118-219): min / max (over the
+ * first 32 * 2^floor(log2(bs/32)) values: the reference's cross-warp
+ * reduction misses the rest when bs/32 is not a power of two), radius =
  * (max - min) / 2, median = min + radius, constant when radius <= bound;
  * otherwise reqLength = 10 + exponent(radius) - exponent(bound) with no
  * clamping, words = bits(x - median) shifted right logically, leading
@@ -87,7 +89,12 @@ size_t orc_cusz_compress(const float* x, size_t n, float eb, int bs, uint8_t* ou
     for (size_t b = 0; b < nb; b++) {
         const float* v = x + b * (size_t)bs;
         float mn, mx;
-        block_range(v, bs, &mn, &mx);
+        /* the reference's cross-warp reduction (xor offsets w/2, w/4, .. 1
+         * over w = bs/32 warps, szx/src/cuszx_float.cu:248-256) reaches the
+         * first 2^floor(log2 w) warps only */
+        int wc = 1;
+        while (2 * wc <= bs / 32) wc *= 2;
+        block_range(v, 32 * wc, &mn, &mx);
         const float radius = (mx - mn) / 2;
         med[b] = mn + radius;
         st[b] = radius <= eb ? 0 : 1;
@@ -113,7 +120,12 @@ size_t orc_cusz_compress(const float* x, size_t n, float eb, int bs, uint8_t* ou
         if (!st[b]) continue;
         const float* v = x + b * (size_t)bs;
         float mn, mx;
-        block_range(v, bs, &mn, &mx);
+        /* the reference's cross-warp reduction (xor offsets w/2, w/4, .. 1
+         * over w = bs/32 warps, szx/src/cuszx_float.cu:248-256) reaches the
+         * first 2^floor(log2 w) warps only */
+        int wc = 1;
+        while (2 * wc <= bs / 32) wc *= 2;
+        block_range(v, 32 * wc, &mn, &mx);
         const float rad = (mx - mn) / 2;
         const int reqLength = 9 + expo(f2u(rad)) - expo(f2u(eb)) + 1;
         int R, rsb;

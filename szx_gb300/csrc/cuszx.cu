@@ -79,6 +79,11 @@ __global__ void __launch_bounds__(kCzThreads) k_cz_blocks(const float* __restric
     const unsigned long long w0 = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nw = (gridDim.x * (unsigned long long)blockDim.x) >> 5;
     const int J = bs / 32, ncb = bs / 4, msize = 5 + ncb;
+    // The reference combines its warps' minima with xor offsets J/2, J/4, ..
+    // 1 (szx/src/cuszx_float.cu:248-256): the lane that keeps the result sees
+    // the first 2^floor(log2 J) warps only (all of them when J is a power of
+    // two), so only their values enter a block's range.
+    const int Jc = 1 << (31 - __clz(J));
     for (unsigned long long b = w0; b < nb; b += nw) {
         const float* xb = x + b * (unsigned long long)bs;
         float v[kCzMaxJ];
@@ -87,8 +92,10 @@ __global__ void __launch_bounds__(kCzThreads) k_cz_blocks(const float* __restric
         for (int j = 0; j < kCzMaxJ; j++)
             if (j < J) {
                 v[j] = xb[j * 32 + lane];
-                mn = fminf(mn, v[j]);
-                mx = fmaxf(mx, v[j]);
+                if (j < Jc) {
+                    mn = fminf(mn, v[j]);
+                    mx = fmaxf(mx, v[j]);
+                }
             }
 #pragma unroll
         for (int d = 16; d; d >>= 1) {

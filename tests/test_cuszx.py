@@ -1,12 +1,19 @@
 """cuSZx ABI (include/cuszx_entry.h): the reference's GPU codec format.
 
 The oracle (oracle/cuszx_oracle.c) restates the reference's cuSZx kernels and
-host code from their source; no reference output is available for this
-format on this machine (the reference's cuSZx is CUDA and its sources are not
-present where the GPU runs), so parity here is with the restatement.  The
-CPU tests pin the restatement's own properties (round trips within the
-bound, the reference's documented corner cases); the GPU tests require the
-library's streams and decodes to equal the oracle's bit for bit.
+host code from their source, and is pinned to golden vectors the reference's
+own cuSZx codec made on a GB300 (tests/golden/cuszx_golden.json, from
+tests/golden/make_cuszx_golden.py: 80 cases, 5 fields x 2 sizes x blockSize
+32/64/128/224 x 2 bounds): every stream and every decode equals the
+reference's, byte for byte.  The CPU tests pin the oracle to those vectors
+and its own corner cases; the GPU tests require the library's streams and
+decodes to equal the golden vectors and the oracle's bit for bit.
+
+The reference's block range covers the first 32 * 2^floor(log2(bs/32))
+values only (its cross-warp reduction, szx/src/cuszx_float.cu:248-256), so
+at blockSize 224 (7 warps: the first 128 values) a block can be declared
+constant or given too few bits and break the bound; the bound holds when
+bs/32 is a power of two.
 """
 import ctypes as C
 
@@ -35,11 +42,55 @@ def test_oracle_round_trips_within_the_bound():
     f = _fields(1)
     for name, eb in SOUND:
         x = f[name]
-        for bs in (32, 64, 128, 224):
+        for bs in (32, 64, 128):
             s = O.cusz_compress(x, eb, bs)
             y = O.cusz_decompress(s, x.size)
             assert np.abs(y.astype(np.float64) - x).max() <= eb, (name, bs, eb)
             assert s[:5] == bytes([1, 1, 1, 0, bs])
+
+
+def _golden():
+    import hashlib
+    import json
+    import os
+    import sys
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    import make_cuszx_golden as M
+    with open(os.path.join(here, "cuszx_golden.json")) as f:
+        g = json.load(f)
+    for c in g["cases"]:
+        x = M.make_field(c["field"], c["n"], c["seed"])
+        assert hashlib.sha256(x.view(np.uint8)).hexdigest() == c["x_sha256"], c["name"]
+        yield c, x
+
+
+def _sha(b):
+    import hashlib
+    return hashlib.sha256(bytes(b)).hexdigest()
+
+
+def test_oracle_matches_the_reference_cuszx_golden_vectors():
+    n = 0
+    for c, x in _golden():
+        s = O.cusz_compress(x, c["eb"], c["bs"])
+        assert len(s) == c["stream_len"] and _sha(s) == c["stream_sha256"], c["name"]
+        y = O.cusz_decompress(s, x.size)
+        assert _sha(y.view(np.uint8)) == c["decode_sha256"], c["name"]
+        n += 1
+    assert n == 80
+
+
+def test_the_reference_block_range_stops_at_a_power_of_two_of_warps():
+    """blockSize 224: a block whose last 96 values move while its first 128
+    are flat is constant for the reference (and decodes to the median)."""
+    x = np.zeros(224, np.float32)
+    x[128:] = 0.5
+    s = O.cusz_compress(x, 0.01, 224)
+    assert s[5:13] == (1).to_bytes(8, "big")          # one constant block
+    assert np.array_equal(O.cusz_decompress(s, 224), np.zeros(224, np.float32))
+    s = O.cusz_compress(x, 0.01, 32)
+    assert O.cusz_decompress(s, 224)[200] == np.float32(0.5)
 
 
 def test_oracle_reproduces_the_reference_corner_cases():
@@ -137,3 +188,18 @@ def test_short_inputs_and_refused_block_sizes(lib):
     o0 = 13 + (nb + 7) // 8 + 4 * (50_000 % 64) + 4 * int.from_bytes(bytes(s[5:13]), "big")
     s[o0:o0 + 2] = (4 * 64).to_bytes(2, "little")
     assert _decompress(L, libc, bytes(s), 50_000) is None
+
+
+@pytest.mark.gpu
+def test_library_matches_the_reference_cuszx_golden_vectors(lib):
+    """The library's cuSZx entry points against what the reference's own cuSZx
+    codec produced for the same inputs: streams and decodes byte for byte."""
+    L, libc = lib
+    n = 0
+    for c, x in _golden():
+        s = _compress(L, libc, x, c["eb"], c["bs"])
+        assert s is not None and len(s) == c["stream_len"] and _sha(s) == c["stream_sha256"], c["name"]
+        y = _decompress(L, libc, s, x.size)
+        assert y is not None and _sha(y.view(np.uint8)) == c["decode_sha256"], c["name"]
+        n += 1
+    assert n == 80
