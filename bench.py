@@ -362,7 +362,10 @@ def run_ours(args, wl, rank, world, local_rank):
         launches = int(launches)
 
     # ---- e2e through the reference-facing entry points, pageable host buffers
-    xh = x.cpu().numpy()                       # ordinary (pageable) host memory, as a drop-in caller has
+    # ordinary (pageable) host memory written by the CPU, as a drop-in
+    # caller's array is: allocated by numpy, filled by a CPU copy
+    xh = np.empty(n, np.float32)
+    np.copyto(xh, x.cpu().numpy())
     free = libc().free
     sz = C.c_size_t()
 

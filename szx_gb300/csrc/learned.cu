@@ -1041,7 +1041,10 @@ __global__ void k_lfx_range_out(const uint32_t* mm, int nf, float* range) {
 }
 
 // Feature rows (after lfx_sample): the two per-row probe windows, then the rows.
-cudaError_t lfx_rows(SZxG_Batch* b, int nrows, const int* h_rows, const float* h_tgt, float* d_X, cudaStream_t s) {
+// second = false skips the second sample's probes (feature 3 is then not
+// meaningful): for callers that only need the crossing (feature 1).
+cudaError_t lfx_rows(SZxG_Batch* b, int nrows, const int* h_rows, const float* h_tgt, float* d_X, cudaStream_t s,
+                     bool second = true) {
     LfxWork* w = b->lfx;
     std::vector<unsigned long long> rt(nrows + 1);
     unsigned long long items = 0;
@@ -1067,8 +1070,9 @@ cudaError_t lfx_rows(SZxG_Batch* b, int nrows, const int* h_rows, const float* h
         TraceScope tr("lfx_probe", s);
         k_lfx_probe<<<lfx_grid(items), 256, 0, s>>>(w->d_f, w->mm, nrows, w->rows, w->mu, 1, w->rtile0, items,
                                                     w->racc, kFine, 0);
-        k_lfx_probe<<<lfx_grid(items), 256, 0, s>>>(w->d_f, w->mm, nrows, w->rows, w->mu, 1, w->rtile0, items,
-                                                    w->racc, 2 * kFine, kOff2);
+        if (second)
+            k_lfx_probe<<<lfx_grid(items), 256, 0, s>>>(w->d_f, w->mm, nrows, w->rows, w->mu, 1, w->rtile0, items,
+                                                        w->racc, 2 * kFine, kOff2);
     }
     const int n = std::max(nrows, b->nf);
     k_lfx_rows<<<(n + 127) / 128, 128, 0, s>>>(w->d_f, w->acc, w->mm, nrows, w->rows, w->tgt, w->mq, w->mu, w->racc,
@@ -1140,11 +1144,13 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
     std::vector<float> range(nf), pred(nf, 0.f), tgt(targetRatio, targetRatio + nf);
     // ys (feature 1) of the fields in fl for targets t[f]; their rows stay in lfx->X, in fl's order
     std::vector<float> col(nf), tsub(nf);
-    auto crossing = [&](const std::vector<int>& fl, const std::vector<float>& t, std::vector<double>& ys) {
+    // (second: with the second sample's probes, for rows the network reads)
+    auto crossing = [&](const std::vector<int>& fl, const std::vector<float>& t, std::vector<double>& ys,
+                        bool second) {
         const int nr = (int)fl.size();
         if (nr == 0) return cudaSuccess;
         for (int k = 0; k < nr; k++) tsub[k] = t[fl[k]];
-        cudaError_t e2 = lfx_rows(b, nr, fl.data(), tsub.data(), b->lfx->X, s);
+        cudaError_t e2 = lfx_rows(b, nr, fl.data(), tsub.data(), b->lfx->X, s, second);
         if (e2 == cudaSuccess)
             e2 = cudaMemcpy2DAsync(col.data(), sizeof(float), b->lfx->X + 1, sizeof(float) * kF, sizeof(float), nr,
                                    cudaMemcpyDeviceToHost, s);
@@ -1174,7 +1180,7 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
     // band (a smaller correction cannot change the outcome much)
     std::vector<double> ys(nf, 0.0);
     std::vector<float> aim = tgt;   // the target each field's sampled crossing was last taken for
-    if (mlp && e == cudaSuccess) e = crossing(all, tgt, ys);
+    if (mlp && e == cudaSuccess) e = crossing(all, tgt, ys, true);
     if (mlp && e == cudaSuccess) e = predict_miss(pred);
     if (mlp && e == cudaSuccess) {
         std::vector<int> moved;
@@ -1186,7 +1192,7 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
                 moved.push_back(f);
             }
         }
-        e = crossing(moved, aim, ys);
+        e = crossing(moved, aim, ys, false);
     }
     if (e != cudaSuccess) return fail_code(e);
 
@@ -1269,7 +1275,7 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
                     if (!(t2[f] > 0.f) || !std::isfinite(t2[f])) t2[f] = aim[f];
                     fl.push_back(f);
                 }
-            if ((e = crossing(fl, t2, ys)) != cudaSuccess) return fail_code(e);
+            if ((e = crossing(fl, t2, ys, false)) != cudaSuccess) return fail_code(e);
             for (int f : fl) {
                 stage[f] = 2;
                 y[f] = (ys[f] > lo[f] && ys[f] < hi[f]) ? ys[f] : next_y(f);
