@@ -692,6 +692,34 @@ __device__ __forceinline__ unsigned long long prefix_resolve_win(unsigned long l
     return pa;
 }
 
+// Copy n bytes from a 16-aligned staging buffer (data at offset 0) to global
+// dst of any alignment with the whole CTA: 16-byte aligned stores, the
+// staging words realigned with funnel shifts; byte copies at the ragged ends.
+__device__ __forceinline__ void cta_copy_realign(const uint8_t* stg, uint32_t n, uint8_t* dst) {
+    if (n == 0) return;
+    const uint32_t sh = (uint32_t)((uintptr_t)dst & 15);
+    uint8_t* gbase = dst - sh;
+    const uint32_t end = sh + n, nch = (end + 15) >> 4;
+    const uint32_t* sw = (const uint32_t*)stg;
+    const uint32_t rs = ((16u - sh) & 3u) * 8u;   // byte phase of staging vs. destination words
+    for (uint32_t c = threadIdx.x; c < nch; c += blockDim.x) {
+        const uint32_t lo = c << 4;
+        if (lo >= sh && lo + 16 <= end) {
+            const uint32_t so = lo - sh, w = so >> 2;
+            const uint32_t a0 = sw[w], a1 = sw[w + 1], a2 = sw[w + 2], a3 = sw[w + 3], a4 = sw[w + 4];
+            *(uint4*)(gbase + lo) = make_uint4(__funnelshift_r(a0, a1, rs), __funnelshift_r(a1, a2, rs),
+                                               __funnelshift_r(a2, a3, rs), __funnelshift_r(a3, a4, rs));
+        }
+    }
+    if (threadIdx.x < 32) {
+        const uint32_t last = nch - 1;
+        const uint32_t c = threadIdx.x < 16 ? 0 : last;
+        const bool part = threadIdx.x < 16 ? (sh > 0 || end < 16) : (last > 0 && (end & 15) != 0);
+        const uint32_t gb = (c << 4) + (threadIdx.x & 15);
+        if (part && gb >= sh && gb < end) gbase[gb] = stg[gb - sh];
+    }
+}
+
 // 16-byte asynchronous global -> shared copies (cp.async, the LSU path: they
 // do not queue behind the TMA unit's bulk copies), L2 only.
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {

@@ -138,17 +138,16 @@ struct NbEncArgs {
     StreamResult* res;
 };
 
-__device__ __forceinline__ void or_bytes_nb(uint32_t* buf, uint32_t q, unsigned long long ev, int cnt) {
-    if (cnt <= 0) return;
-    uint32_t sh = (q & 3) * 8;
-    uint32_t* w = buf + (q >> 2);
-    unsigned long long lo = ev << sh;
-    atomicOr(w, (uint32_t)lo);
-    int span = (int)(q & 3) + cnt;
-    if (span > 4) atomicOr(w + 1, (uint32_t)(lo >> 32));
-    if (span > 8) atomicOr(w + 2, (uint32_t)(ev >> (64 - sh)));
-}
-
+// One pass over the input in tiles of kNbTile values taken from an atomic
+// counter.  Per tile: the values (loaded during the previous tile's
+// placement), shifted words and lead codes (one XOR chain over the whole
+// array: a thread's first value's predecessor is the previous thread's last,
+// or the value before the tile), a CTA scan of the stored-byte counts, the
+// tile's byte count published to the look-back, the lead codes written to
+// their fixed place, the mid bytes emitted into shared memory with byte
+// stores at tile-local offsets; then the look-back resolves the tile's
+// offset (its predecessors have had the emission to publish) and the CTA
+// copies the bytes out, realigned.  The next tile is claimed a tile ahead.
 template <typename T>
 __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
     using EL = Elem<T>;
@@ -156,7 +155,7 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
     constexpr int W = EL::W;
     __shared__ __align__(16) uint8_t stage[kNbTile * W + 48];
     __shared__ uint32_t s_sum[8];
-    __shared__ long long s_tile;
+    __shared__ long long s_tile[2];
     __shared__ unsigned long long s_base;
     __shared__ int s_skip;
     const T* x = (const T*)a.x;
@@ -175,14 +174,22 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
     uint8_t* mid = lead + L;
     const unsigned long long mid_cap = a.cap - (kNbShift + 17 + L);
     const int lane = threadIdx.x & 31;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(a.tile_ctr, 1ull);
-        __syncthreads();
-        const long long tile = s_tile;
-        if (tile >= (long long)a.ntiles) break;
+    const int low = 8 * (W - R);
+    if (threadIdx.x == 0) s_tile[0] = (long long)atomicAdd(a.tile_ctr, 1ull);
+    __syncthreads();
+    long long tile = s_tile[0];
+    T v[kNbPer];
+    T before = (T)0;   // lane 0: the value before its first one
+    auto fetch = [&](long long t, T (&dst)[kNbPer], T& bef) {
+        const unsigned long long first = (unsigned long long)t * kNbTile + threadIdx.x * kNbPer;
+        load16<T>(x, first, a.n, dst);
+        bef = (lane == 0 && first > 0 && first - 1 < a.n) ? x[first - 1] : (T)0;
+    };
+    if (tile < (long long)a.ntiles) fetch(tile, v, before);
+    for (int it = 0; tile < (long long)a.ntiles; it++) {
+        // the tile after this one, claimed now and read after the scan's barriers
+        if (threadIdx.x == 0) s_tile[(it + 1) & 1] = (long long)atomicAdd(a.tile_ctr, 1ull);
         const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
-        T v[kNbPer];
-        load16<T>(x, first, a.n, v);
         U cur[kNbPer];
         bool bad = false;
 #pragma unroll
@@ -191,31 +198,66 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
             bad |= d != d;
             cur[e] = EL::bits(d) >> s;
         }
-        if (__any_sync(0xffffffffu, bad)) {
+        const T dprev = EL::sub(before, med);
+        U prev_l0 = first > 0 ? (EL::bits(dprev) >> s) : (U)0;
+        if (__any_sync(0xffffffffu, bad || (lane == 0 && first > 0 && dprev != dprev))) {
 #pragma unroll
             for (int e = 0; e < kNbPer; e++) cur[e] = EL::bits(xsub(v[e], med)) >> s;
+            if (lane == 0 && first > 0) prev_l0 = EL::bits(xsub(before, med)) >> s;
         }
         U prev = __shfl_up_sync(0xffffffffu, cur[kNbPer - 1], 1);
-        if (lane == 0) prev = first > 0 && first - 1 < a.n ? (EL::bits(xsub(x[first - 1], med)) >> s) : (U)0;
-        uint32_t codes = 0, mine = 0;
+        if (lane == 0) prev = prev_l0;
+        uint32_t codes = 0, mine = 0, cnt4[kNbPer / 4];
 #pragma unroll
-        for (int e = 0; e < kNbPer; e++) {
-            U xr = cur[e] ^ (e ? cur[e - 1] : prev);
-            int lz;
-            if constexpr (sizeof(T) == 4) lz = __clz(xr) >> 3;
-            else lz = __clzll((long long)xr) >> 3;
-            int ld = lz < 3 ? lz : 3;
-            if (first + e < a.n) {
-                codes |= (uint32_t)ld << (8 * (e >> 2) + 6 - 2 * (e & 3));
-                int c = R - ld;
-                mine += c > 0 ? c : 0;
+        for (int k = 0; k < kNbPer / 4; k++) {
+            uint32_t c4 = 0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int e = 4 * k + i;
+                const U xr = cur[e] ^ (e ? cur[e - 1] : prev);
+                int lz;
+                if constexpr (sizeof(T) == 4) lz = __clz(xr) >> 3;
+                else lz = __clzll((long long)xr) >> 3;
+                const int ld = lz < 3 ? lz : 3;
+                if (first + e < a.n) {
+                    codes |= (uint32_t)ld << (8 * k + 6 - 2 * i);
+                    const int c = R - ld;
+                    c4 |= (uint32_t)(c > 0 ? c : 0) << (8 * i);
+                }
             }
+            cnt4[k] = c4;
+            mine += (c4 * 0x01010101u) >> 24;
         }
         uint32_t total;
-        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);
+        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // two barriers
+        if (threadIdx.x < 32) lookback_publish(a.st, tile, total, 0);
+        // lead codes: 4 bytes per thread, at their fixed place
+        const unsigned long long lb = first >> 2;
+        if (lb + 4 <= L && ((uintptr_t)(lead + lb) & 3) == 0) *(uint32_t*)(lead + lb) = codes;
+        else
+            for (int j = 0; j < 4; j++)
+                if (lb + j < L) lead[lb + j] = (uint8_t)(codes >> (8 * j));
+        // mid bytes: each value's low (R - lead) bytes of its word shifted down
+        // to the stored range, at tile-local offsets (every byte written once)
+        uint32_t q = ex;
+#pragma unroll
+        for (int k = 0; k < kNbPer / 4; k++) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const uint32_t c = byte_of(cnt4[k], i);
+                const U ev = cur[4 * k + i] >> low;
+#pragma unroll
+                for (int j = 0; j < W; j++)
+                    if ((uint32_t)j < c) stage[q + j] = (uint8_t)(ev >> (8 * j));
+                q += c;
+            }
+        }
+        // the next tile's values are in flight during the look-back
+        const long long next = s_tile[(it + 1) & 1];
+        if (next < (long long)a.ntiles) fetch(next, v, before);
         if (threadIdx.x < 32) {
             unsigned long long base, dummy;
-            lookback_wide(a.st, tile, total, 0, &base, &dummy, a.err);
+            lookback_resolve(a.st, tile, total, 0, &base, &dummy, a.err);
             if (threadIdx.x == 0) {
                 s_base = base;
                 const bool ok = base + total <= mid_cap;
@@ -238,37 +280,10 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
                 }
             }
         }
-        __syncthreads();   // s_base / s_skip from the look-back
-        // lead codes: 4 bytes per thread
-        const unsigned long long lb = first >> 2;
-        if (lb + 4 <= L && ((uintptr_t)(lead + lb) & 3) == 0) *(uint32_t*)(lead + lb) = codes;
-        else
-            for (int j = 0; j < 4; j++)
-                if (lb + j < L) lead[lb + j] = (uint8_t)(codes >> (8 * j));
-        // mid bytes via shared staging
-        const unsigned long long base = s_base;
-        const uint32_t sh = (uint32_t)((uintptr_t)(mid + base) & 15);
-        const uint32_t nz = (sh + total + 16 + 15) >> 4;
-        for (uint32_t i = threadIdx.x; i < nz; i += kNbThreads) ((uint4*)stage)[i] = make_uint4(0, 0, 0, 0);
-        __syncthreads();
-        if (!s_skip) {
-            uint32_t q = sh + ex;
-            uint32_t* buf = (uint32_t*)stage;
-#pragma unroll
-            for (int e = 0; e < kNbPer; e++) {
-                int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
-                int c = R - ld;
-                if (first + e < a.n && c > 0) {
-                    unsigned long long ev = (unsigned long long)(cur[e] >> (8 * (W - R)));
-                    ev &= c >= 8 ? ~0ull : ((1ull << (8 * c)) - 1);
-                    or_bytes_nb(buf, q, ev, c);
-                    q += c;
-                }
-            }
-        }
-        __syncthreads();
-        if (!s_skip) cta_copy_out(stage, sh, total, mid + base);
-        __syncthreads();
+        __syncthreads();   // the tile's bytes are staged, its offset known
+        if (!s_skip) cta_copy_realign(stage, total, mid + s_base);
+        __syncthreads();   // the staging buffer and s_base are free again
+        tile = next;
     }
 }
 
@@ -291,7 +306,18 @@ cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t
     a.tile_ctr = &ws.counters[0];
     a.err = ws.err;
     a.res = ws.result;
-    size_t g = (size_t)sm_count() * (dtype == 0 ? 6 : 4);
+    static int per_sm[2][64] = {{0}};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    int& occ = per_sm[dtype == 0 ? 0 : 1][dev];
+    if (!occ) {
+        if (dtype == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nb_encode<float>, kNbThreads, 0);
+        else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nb_encode<double>, kNbThreads, 0);
+        if (e != cudaSuccess) return e;
+        if (occ < 1) occ = 1;
+    }
+    size_t g = (size_t)sm_count() * occ;
     int grid = (int)(ntiles < g ? ntiles : g);
     {
         TraceScope tr("nonblocked_encode", s);
