@@ -139,23 +139,36 @@ struct NbEncArgs {
 };
 
 // One pass over the input in tiles of kNbTile values taken from an atomic
-// counter.  Per tile: the values (loaded during the previous tile's
-// placement), shifted words and lead codes (one XOR chain over the whole
-// array: a thread's first value's predecessor is the previous thread's last,
-// or the value before the tile), a CTA scan of the stored-byte counts, the
-// tile's byte count published to the look-back, the lead codes written to
-// their fixed place, the mid bytes emitted into shared memory with byte
-// stores at tile-local offsets; then the look-back resolves the tile's
-// offset (its predecessors have had the emission to publish) and the CTA
-// copies the bytes out, realigned.  The next tile is claimed a tile ahead.
+// counter, one tile ahead.  Per tile T_j: the values (loaded during the
+// previous iteration), shifted words and lead codes (one XOR chain over the
+// whole array: a thread's first value's predecessor is the previous
+// thread's last, or the value before the tile), a CTA scan of the
+// stored-byte counts, the tile's byte count published to the look-back, the
+// lead codes written to their fixed place, the mid bytes emitted into one of
+// two shared staging buffers with byte stores at tile-local offsets.  T_{j-1}
+// is placed one iteration late: its offset is the inclusive prefix of this
+// CTA's previous tile (known here) plus the counts of the tiles claimed in
+// between, read from a window of status words copied in with cp.async at the
+// start of the iteration (a window with unpublished words is copied again a
+// few times, then the global look-back takes over); then the CTA copies
+// T_{j-1}'s bytes out, realigned.
+constexpr int kNbWin = 1024;   // status words per placement window (4 KiB)
+constexpr int kNbRepolls = 32;
+
 template <typename T>
-__global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
+constexpr int nb_stage_bytes() { return ((kNbTile * (int)sizeof(T) + 48) + 15) / 16 * 16; }
+
+template <typename T>
+__global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encode(NbEncArgs a) {
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
-    __shared__ __align__(16) uint8_t stage[kNbTile * W + 48];
+    extern __shared__ __align__(16) uint8_t nb_dyn[];   // two staging buffers of nb_stage_bytes<T>()
+    auto stage = [&](int k) { return nb_dyn + (k & 1) * nb_stage_bytes<T>(); };
+    __shared__ __align__(16) uint32_t s_win[kNbWin + 8];
     __shared__ uint32_t s_sum[8];
     __shared__ long long s_tile[2];
+    __shared__ uint32_t s_total[2];
     __shared__ unsigned long long s_base;
     __shared__ int s_skip;
     const T* x = (const T*)a.x;
@@ -175,20 +188,106 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
     const unsigned long long mid_cap = a.cap - (kNbShift + 17 + L);
     const int lane = threadIdx.x & 31;
     const int low = 8 * (W - R);
+    const long long nt = (long long)a.ntiles;
+    // warp 0's placement state: anchor tile and its inclusive prefix; window
+    long long an_t = -1;
+    unsigned long long an_incl = 0;
+    long long w_lo = 0;
+    int w_ok = 0;
+    // warp 0: copy the status words of the tiles between the anchor and t
+    auto win_issue = [&](long long t) {
+        w_ok = 0;
+        if (an_t >= 0 && an_t < t && t - an_t - 1 <= kNbWin) {
+            if (t - an_t == 1) {
+                w_ok = 2;
+            } else {
+                w_lo = (an_t + 1) & ~3ll;
+                const int units = (int)((t - w_lo + 3) >> 2);
+                for (int u = lane; u < units; u += 32) cp_async16(&s_win[4 * u], a.st.st + w_lo + 4 * u);
+                w_ok = 1;
+            }
+        }
+    };
+    // warp 0: offset of tile t (count agg), its inclusive prefix published
+    auto place = [&](long long t, uint32_t agg) {
+        unsigned long long base = 0;
+        bool placed = t == 0;
+        if (!placed && w_ok == 2) {
+            base = an_incl;
+            placed = true;
+        } else if (!placed && w_ok == 1) {
+            const int units = (int)((t - w_lo + 3) >> 2);
+            for (int attempt = 0;; attempt++) {
+                cp_async_wait_all();
+                __syncwarp();
+                unsigned long long sum = 0;
+                bool ready = true;
+                for (long long i = an_t + 1 + lane; i < t; i += 32) {
+                    const uint32_t w = s_win[i - w_lo];
+                    ready = ready && (w & 0xC0000000u) != 0;
+                    sum += w & 0x7FFFFFu;
+                }
+                if (__all_sync(0xffffffffu, ready)) {
+                    base = an_incl + warp_sum(sum);
+                    placed = true;
+                    break;
+                }
+                if (attempt == kNbRepolls) break;
+                __nanosleep(128);
+                for (int u = lane; u < units; u += 32) cp_async16(&s_win[4 * u], a.st.st + w_lo + 4 * u);
+            }
+        }
+        if (!placed) {
+            unsigned long long dummy;
+            lookback_resolve(a.st, t, agg, 0, &base, &dummy, a.err);   // publishes t's inclusive prefix
+        } else if (t > 0 && lane == 0) {
+            __stcg(&a.st.inc_a[t], base + agg);
+            __stcg(&a.st.inc_b[t], 0ull);
+            __threadfence();
+            st_volatile32(&a.st.st[t], kSt32Inc | (agg & 0x7FFFFFu));
+        }
+        an_t = t;
+        an_incl = base + agg;
+        if (lane == 0) {
+            s_base = base;
+            const bool ok = base + agg <= mid_cap;
+            s_skip = !ok;
+            if (!ok) atomicExch(a.err, kErrCapacity);
+            if (t == nt - 1) {
+                uint8_t* h = a.out + kNbShift;
+                h[0] = 1; h[1] = 1; h[2] = 1; h[3] = 0;
+                h[4] = (uint8_t)reqLength;
+                h[5] = (uint8_t)(med_stored >> 24); h[6] = (uint8_t)(med_stored >> 16);
+                h[7] = (uint8_t)(med_stored >> 8); h[8] = (uint8_t)med_stored;
+                for (int k = 0; k < 8; k++) h[9 + k] = (uint8_t)(L >> (56 - 8 * k));
+                StreamResult r;
+                r.offset = kNbShift;
+                r.size = 17 + L + base + agg;
+                r.nb_const = 0;
+                r.eb = P.eb;
+                r.status = 0;
+                *a.res = r;
+            }
+        }
+    };
     if (threadIdx.x == 0) s_tile[0] = (long long)atomicAdd(a.tile_ctr, 1ull);
     __syncthreads();
     long long tile = s_tile[0];
+    long long t1 = -1;   // T_{j-1}, waiting for its placement
     T v[kNbPer];
-    T before = (T)0;   // lane 0: the value before its first one
-    auto fetch = [&](long long t, T (&dst)[kNbPer], T& bef) {
+    T before = (T)0;     // lane 0: the value before its first one
+    auto fetch = [&](long long t) {
         const unsigned long long first = (unsigned long long)t * kNbTile + threadIdx.x * kNbPer;
-        load16<T>(x, first, a.n, dst);
-        bef = (lane == 0 && first > 0 && first - 1 < a.n) ? x[first - 1] : (T)0;
+        load16<T>(x, first, a.n, v);
+        before = (lane == 0 && first > 0 && first - 1 < a.n) ? x[first - 1] : (T)0;
     };
-    if (tile < (long long)a.ntiles) fetch(tile, v, before);
-    for (int it = 0; tile < (long long)a.ntiles; it++) {
-        // the tile after this one, claimed now and read after the scan's barriers
+    if (tile < nt) fetch(tile);
+    int it = 0;
+    for (; tile < nt; it++) {
+        // the next tile, claimed now and read after the scan's barriers
         if (threadIdx.x == 0) s_tile[(it + 1) & 1] = (long long)atomicAdd(a.tile_ctr, 1ull);
+        // T_{j-1}'s window, in flight during this tile's work
+        if (threadIdx.x < 32 && t1 >= 0) win_issue(t1);
         const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
         U cur[kNbPer];
         bool bad = false;
@@ -231,6 +330,7 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
         uint32_t total;
         const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // two barriers
         if (threadIdx.x < 32) lookback_publish(a.st, tile, total, 0);
+        if (threadIdx.x == 0) s_total[it & 1] = total;
         // lead codes: 4 bytes per thread, at their fixed place
         const unsigned long long lb = first >> 2;
         if (lb + 4 <= L && ((uintptr_t)(lead + lb) & 3) == 0) *(uint32_t*)(lead + lb) = codes;
@@ -239,6 +339,7 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
                 if (lb + j < L) lead[lb + j] = (uint8_t)(codes >> (8 * j));
         // mid bytes: each value's low (R - lead) bytes of its word shifted down
         // to the stored range, at tile-local offsets (every byte written once)
+        uint8_t* stg = stage(it);
         uint32_t q = ex;
 #pragma unroll
         for (int k = 0; k < kNbPer / 4; k++) {
@@ -248,42 +349,28 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_encode(NbEncArgs a) {
                 const U ev = cur[4 * k + i] >> low;
 #pragma unroll
                 for (int j = 0; j < W; j++)
-                    if ((uint32_t)j < c) stage[q + j] = (uint8_t)(ev >> (8 * j));
+                    if ((uint32_t)j < c) stg[q + j] = (uint8_t)(ev >> (8 * j));
                 q += c;
             }
         }
-        // the next tile's values are in flight during the look-back
+        // the next tile's values are in flight during the placement
         const long long next = s_tile[(it + 1) & 1];
-        if (next < (long long)a.ntiles) fetch(next, v, before);
-        if (threadIdx.x < 32) {
-            unsigned long long base, dummy;
-            lookback_resolve(a.st, tile, total, 0, &base, &dummy, a.err);
-            if (threadIdx.x == 0) {
-                s_base = base;
-                const bool ok = base + total <= mid_cap;
-                s_skip = !ok;
-                if (!ok) atomicExch(a.err, kErrCapacity);
-                if (tile == (long long)a.ntiles - 1) {
-                    uint8_t* h = a.out + kNbShift;
-                    h[0] = 1; h[1] = 1; h[2] = 1; h[3] = 0;
-                    h[4] = (uint8_t)reqLength;
-                    h[5] = (uint8_t)(med_stored >> 24); h[6] = (uint8_t)(med_stored >> 16);
-                    h[7] = (uint8_t)(med_stored >> 8); h[8] = (uint8_t)med_stored;
-                    for (int k = 0; k < 8; k++) h[9 + k] = (uint8_t)(L >> (56 - 8 * k));
-                    StreamResult r;
-                    r.offset = kNbShift;
-                    r.size = 17 + L + base + total;
-                    r.nb_const = 0;
-                    r.eb = P.eb;
-                    r.status = 0;
-                    *a.res = r;
-                }
-            }
-        }
-        __syncthreads();   // the tile's bytes are staged, its offset known
-        if (!s_skip) cta_copy_realign(stage, total, mid + s_base);
-        __syncthreads();   // the staging buffer and s_base are free again
+        if (next < nt) fetch(next);
+        if (threadIdx.x < 32 && t1 >= 0) place(t1, s_total[(it - 1) & 1]);
+        __syncthreads();   // T_j staged; T_{j-1}'s offset known
+        if (t1 >= 0 && !s_skip) cta_copy_realign(stage(it - 1), s_total[(it - 1) & 1], mid + s_base);
+        __syncthreads();   // T_{j-1}'s buffer and s_base are free again
+        t1 = tile;
         tile = next;
+    }
+    // the last tile of this CTA
+    if (t1 >= 0) {
+        if (threadIdx.x < 32) {
+            win_issue(t1);
+            place(t1, s_total[(it - 1) & 1]);
+        }
+        __syncthreads();
+        if (!s_skip) cta_copy_realign(stage(it - 1), s_total[(it - 1) & 1], mid + s_base);
     }
 }
 
@@ -311,9 +398,17 @@ cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     int& occ = per_sm[dtype == 0 ? 0 : 1][dev];
+    const size_t dyn = 2 * (size_t)(dtype == 0 ? nb_stage_bytes<float>() : nb_stage_bytes<double>());
     if (!occ) {
-        if (dtype == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nb_encode<float>, kNbThreads, 0);
-        else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nb_encode<double>, kNbThreads, 0);
+        if (dtype == 0) {
+            e = cudaFuncSetAttribute(k_nb_encode<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nb_encode<float>, kNbThreads, dyn);
+        } else {
+            e = cudaFuncSetAttribute(k_nb_encode<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nb_encode<double>, kNbThreads, dyn);
+        }
         if (e != cudaSuccess) return e;
         if (occ < 1) occ = 1;
     }
@@ -321,8 +416,8 @@ cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t
     int grid = (int)(ntiles < g ? ntiles : g);
     {
         TraceScope tr("nonblocked_encode", s);
-        if (dtype == 0) k_nb_encode<float><<<grid, kNbThreads, 0, s>>>(a);
-        else k_nb_encode<double><<<grid, kNbThreads, 0, s>>>(a);
+        if (dtype == 0) k_nb_encode<float><<<grid, kNbThreads, dyn, s>>>(a);
+        else k_nb_encode<double><<<grid, kNbThreads, dyn, s>>>(a);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // fold the error word into the result
