@@ -452,204 +452,375 @@ __device__ __forceinline__ uint32_t lead_word(const uint8_t* lead, unsigned long
     return w;
 }
 
-// Per-tile mid-byte count and, for the top three byte lanes, where in the
-// tile's mid bytes the last value storing that lane put it.  Look-back over
-// tiles yields each tile's mid-byte offset and the latest earlier tile that
-// stored each lane.  aux[3t] = offset, aux[3t+1] = latest writer tiles (3x21
-// bits, tile+1), aux[3t+2] = own writer positions (3x21 bits, pos+1).
+// Lead codes of 16 values in one 32-bit word (value e at bits 8*(e/4) + 6 -
+// 2*(e%4)), as masks with one bit per value: m_k has the low bit of value
+// e's pair set when its lead code is <= k, i.e. when its byte lane W-1-k is
+// stored.  vorder() moves value e's bit to position 2e+1 (value order).
+__device__ __forceinline__ uint32_t vorder(uint32_t m) { return __byte_perm(__brev(m), 0, 0x0123); }
+
+// Valid-value mask (pair low bits) of a word whose first value is `first`.
+__device__ __forceinline__ uint32_t valid_pairs(unsigned long long first, unsigned long long n) {
+    if (first + 16 <= n) return 0x55555555u;
+    uint32_t v = 0;
+    for (int e = 0; e < 16; e++)
+        if (first + e < n) v |= 1u << (8 * (e >> 2) + 6 - 2 * (e & 3));
+    return v;
+}
+
+// Lead word of values [first, first + 16): one 4-byte load when aligned.
+__device__ __forceinline__ uint32_t lead_word16(const uint8_t* lead, unsigned long long first,
+                                                unsigned long long L) {
+    const unsigned long long lb = first >> 2;
+    if (lb + 4 <= L && ((uintptr_t)(lead + lb) & 3) == 0) return __ldg((const uint32_t*)(lead + lb));
+    return lead_word(lead, lb, L);
+}
+
+// Per tile (one warp): its mid-byte count (tcnt[t]) and, for each of the top
+// three byte lanes, where in the tile's mid bytes the last value storing that
+// lane put it (aux[3t+2], 3x21 bits, position+1, 0 = none).  A lane takes the
+// tile's 16-code words lane, lane+32, ... so that every load of the warp reads
+// 128 consecutive lead bytes; a warp scan per round orders the words.  Counts
+// and positions come from population counts of the per-lane masks:
+// a value stores max(R - lead, 0) bytes = the number of k < R with lead <= k.
+// The CTA's eight tiles form a group: aux[3t] / aux[3t+1] get the tile's
+// exclusive prefix within its group (bytes; latest writer tiles, 3x21 bits,
+// tile+1), gsum[g] / gwr[g] the group's totals.  Independent per group: no
+// look-back.
 template <typename T>
-__global__ void __launch_bounds__(kNbThreads) k_nb_summary(const uint8_t* s, const NonBlockedHdr* hp,
-                                                           unsigned long long* aux, TileStatus32 st,
-                                                           unsigned long long* ctr, int* err) {
+__global__ void __launch_bounds__(kNbThreads) k_nb_count(const uint8_t* __restrict__ s, const NonBlockedHdr* hp,
+                                                         uint32_t* __restrict__ tcnt,
+                                                         unsigned long long* __restrict__ aux,
+                                                         unsigned long long* __restrict__ gsum,
+                                                         unsigned long long* __restrict__ gwr) {
     constexpr int W = Elem<T>::W;
-    __shared__ uint32_t s_sum[8];
-    __shared__ int s_pos[3][8];
-    __shared__ long long s_tile;
+    constexpr int kTpg = kNbThreads / 32;   // tiles per group
+    __shared__ uint32_t s_cnt[kTpg];
+    __shared__ unsigned long long s_own[kTpg];
     const NonBlockedHdr h = *hp;
     if (!h.ok) return;
     int R, sft;
     split_reqlen(h.reqLength, &R, &sft);
     if (R > W) return;
     const unsigned long long ntiles = (h.n + kNbTile - 1) / kNbTile;
-    const uint8_t* lead = s + 17;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(ctr, 1ull);
-        __syncthreads();
-        const long long tile = s_tile;
-        if (tile >= (long long)ntiles) break;
-        const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
-        const uint32_t codes = lead_word(lead, first >> 2, h.L);
-        uint32_t mine = 0;
-        int lpos[3] = {-1, -1, -1};
-        for (int e = 0; e < kNbPer; e++) {
-            if (first + e >= h.n) break;
-            int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
-            int c = R - ld;
-            if (c > 0) {
+    const long long tile = (long long)blockIdx.x * kTpg + warp;
+    const uint8_t* lead = s + 17;
+    const uint32_t full = R > 3 ? (uint32_t)(R - 3) : 0u;   // bytes every value stores below the top three lanes
+    uint32_t run = 0;
+    int gpos[3] = {-1, -1, -1};
+    if (tile < (long long)ntiles) {
+#pragma unroll 2
+        for (int j = 0; j < kNbTile / (32 * kNbPer); j++) {
+            const unsigned long long first =
+                (unsigned long long)tile * kNbTile + (unsigned long long)kNbPer * (32 * j + lane);
+            const uint32_t codes = lead_word16(lead, first, h.L);
+            const uint32_t valid = valid_pairs(first, h.n);
+            const uint32_t lo = codes & 0x55555555u, hi = (codes >> 1) & 0x55555555u;
+            const uint32_t m0 = ~(lo | hi) & valid, m1 = ~hi & valid, m2 = ~(lo & hi) & valid;
+            const uint32_t nv = __popc(valid);
+            const uint32_t mine = __popc(m0) + (R >= 2 ? __popc(m1) : 0u) + (R >= 3 ? __popc(m2) : 0u) + full * nv;
+            const uint32_t incl = warp_inclusive_sum(mine);
+            const uint32_t ex = run + incl - mine;
+            const uint32_t v0 = vorder(m0), v1 = vorder(m1), v2 = vorder(m2);
 #pragma unroll
-                for (int k = 0; k < 3; k++)   // lane W-1-k is stored when ld <= k (and is required when k <= R-1)
-                    if (ld <= k && k <= R - 1) lpos[k] = (int)mine + (R - 1 - k);
-                mine += c;
+            for (int k = 0; k < 3; k++) {
+                const uint32_t vk = k == 0 ? v0 : k == 1 ? v1 : v2;
+                if (k <= R - 1 && vk) {   // later words hold later positions
+                    const int e = (31 - __clz(vk)) >> 1;
+                    const uint32_t below = (1u << (2 * e)) - 1;
+                    const uint32_t before = __popc(v0 & below) + (R >= 2 ? __popc(v1 & below) : 0u) +
+                                            (R >= 3 ? __popc(v2 & below) : 0u) + full * (uint32_t)e;
+                    gpos[k] = (int)(ex + before) + (R - 1 - k);
+                }
             }
+            run += __shfl_sync(0xffffffffu, incl, 31);
         }
-        uint32_t total;
-        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);
-        int gpos[3];
+    }
+    unsigned long long own = 0;
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            int p = lpos[k] >= 0 ? (int)ex + lpos[k] : -1;
+    for (int k = 0; k < 3; k++) {
+        int p = gpos[k];
 #pragma unroll
-            for (int d = 16; d > 0; d >>= 1) p = max(p, __shfl_xor_sync(0xffffffffu, p, d));
-            if (lane == 0) s_pos[k][warp] = p;
-        }
-        __syncthreads();
-        unsigned long long own = 0;
-        uint32_t wrote = 0;
+        for (int d = 16; d > 0; d >>= 1) p = max(p, __shfl_xor_sync(0xffffffffu, p, d));
+        own |= (unsigned long long)(p + 1) << (21 * k);
+    }
+    if (lane == 0) {
+        s_cnt[warp] = run;
+        s_own[warp] = own;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long pa = 0, pb = 0;
+        for (int w = 0; w < kTpg; w++) {
+            const long long t = (long long)blockIdx.x * kTpg + w;
+            if (t >= (long long)ntiles) break;
+            const unsigned long long o = s_own[w];
+            aux[3 * t] = pa;
+            aux[3 * t + 1] = pb;
+            aux[3 * t + 2] = o;
+            tcnt[t] = s_cnt[w];
+            pa += s_cnt[w];
+            unsigned long long wr = 0;
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            int p = -1;
-            for (int w = 0; w < kNbThreads / 32; w++) p = max(p, s_pos[k][w]);
-            gpos[k] = p;
-            own |= (unsigned long long)(p + 1) << (21 * k);
-            if (p >= 0) wrote |= 1u << k;
+            for (int k = 0; k < 3; k++)
+                if ((o >> (21 * k)) & 0x1FFFFF) wr |= (unsigned long long)(t + 1) << (21 * k);
+            pb = Max3x21Op::op(pb, wr);
         }
-        if (threadIdx.x < 32) {
-            unsigned long long base, lw;
-            lookback_wide<WriterPolicy>(st, tile, total, wrote, &base, &lw, err);
-            if (threadIdx.x == 0) {
-                aux[3 * tile] = base;
-                aux[3 * tile + 1] = lw;
-                aux[3 * tile + 2] = own;
-                if (tile == (long long)ntiles - 1 && base + total > h.mid_len) atomicExch(err, kErrStream);
-            }
-        }
-        (void)gpos;
-        __syncthreads();
+        gsum[blockIdx.x] = pa;
+        gwr[blockIdx.x] = pb;
     }
 }
 
+// One CTA: exclusive scan, in place, of the group totals (gsum: bytes, a
+// sum; gwr: latest writer tiles, combined by max), over chunks of
+// kScanThreads * kScanPer groups carried from chunk to chunk.  A stream
+// whose mid bytes run past its end is reported.
+constexpr int kScanThreads = 512, kScanPer = 8;
+
+__global__ void __launch_bounds__(kScanThreads) k_nb_scan(const NonBlockedHdr* hp, unsigned long long* gsum,
+                                                          unsigned long long* gwr, int* err) {
+    __shared__ unsigned long long s_a[kScanThreads / 32], s_b[kScanThreads / 32];
+    const NonBlockedHdr h = *hp;
+    if (!h.ok) return;
+    const unsigned long long ntiles = (h.n + kNbTile - 1) / kNbTile;
+    const unsigned long long ng = (ntiles + kNbThreads / 32 - 1) / (kNbThreads / 32);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned long long ca = 0, cb = 0;   // totals of the earlier chunks
+    for (unsigned long long c0 = 0; c0 < ng; c0 += (unsigned long long)kScanThreads * kScanPer) {
+        const unsigned long long g0 = c0 + (unsigned long long)threadIdx.x * kScanPer;
+        unsigned long long va[kScanPer], vb[kScanPer];
+        unsigned long long la = 0, lb = 0;
+#pragma unroll
+        for (int i = 0; i < kScanPer; i++) {
+            va[i] = g0 + i < ng ? gsum[g0 + i] : 0ull;
+            vb[i] = g0 + i < ng ? gwr[g0 + i] : 0ull;
+            la += va[i];
+            lb = Max3x21Op::op(lb, vb[i]);
+        }
+        unsigned long long ia = la, ib = lb;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long oa = __shfl_up_sync(0xffffffffu, ia, d);
+            const unsigned long long ob = __shfl_up_sync(0xffffffffu, ib, d);
+            if (lane >= d) {
+                ia += oa;
+                ib = Max3x21Op::op(ob, ib);
+            }
+        }
+        if (lane == 31) {
+            s_a[warp] = ia;
+            s_b[warp] = ib;
+        }
+        __syncthreads();
+        unsigned long long pa = ca, pb = cb, ta = ca, tb = cb;
+        for (int w = 0; w < kScanThreads / 32; w++) {
+            if (w < warp) {
+                pa += s_a[w];
+                pb = Max3x21Op::op(pb, s_b[w]);
+            }
+            ta += s_a[w];
+            tb = Max3x21Op::op(tb, s_b[w]);
+        }
+        unsigned long long ea = __shfl_up_sync(0xffffffffu, ia, 1), eb = __shfl_up_sync(0xffffffffu, ib, 1);
+        if (lane == 0) {
+            ea = 0;
+            eb = 0;
+        }
+        pa += ea;
+        pb = Max3x21Op::op(pb, eb);
+#pragma unroll
+        for (int i = 0; i < kScanPer; i++) {
+            if (g0 + i < ng) {
+                gsum[g0 + i] = pa;
+                gwr[g0 + i] = pb;
+            }
+            pa += va[i];
+            pb = Max3x21Op::op(pb, vb[i]);
+        }
+        ca = ta;
+        cb = tb;
+        __syncthreads();   // s_a / s_b are read before the next chunk writes them
+    }
+    if (threadIdx.x == 0 && ca > h.mid_len) atomicExch(err, kErrStream);
+}
+
+// One thread per tile: the bytes that the top three byte lanes carry into the
+// tile (the last earlier value that stored each lane), read from the stream
+// and packed into aux[3t+1] (lane W-1-k at bits 8*(2-k)).  A tile's offset is
+// its group's prefix (gsum) plus its offset in the group (aux[3t]); each
+// thread rewrites only its own tile's aux[3t+1] and reads only the other two
+// words of other tiles.
+__global__ void k_nb_carry(const uint8_t* __restrict__ s, unsigned long long len, const NonBlockedHdr* hp,
+                           unsigned long long* aux, const unsigned long long* __restrict__ gsum,
+                           const unsigned long long* __restrict__ gwr) {
+    constexpr int kTpg = kNbThreads / 32;
+    const NonBlockedHdr h = *hp;
+    if (!h.ok) return;
+    const unsigned long long ntiles = (h.n + kNbTile - 1) / kNbTile;
+    const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    const unsigned long long lw = Max3x21Op::op(gwr[t / kTpg], aux[3 * t + 1]);
+    uint32_t carry = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const unsigned long long t1 = (lw >> (21 * k)) & 0x1FFFFF;
+        if (t1) {
+            const unsigned long long u = t1 - 1;
+            const unsigned long long p1 = (aux[3 * u + 2] >> (21 * k)) & 0x1FFFFF;
+            const unsigned long long pos = h.mid_off + gsum[u / kTpg] + aux[3 * u] + (p1 - 1);
+            const uint32_t byte = pos < len ? s[pos] : 0u;
+            carry |= byte << (8 * (2 - k));
+        }
+    }
+    aux[3 * t + 1] = carry;
+}
+
+// Decode, tiles taken in a fixed order (blockIdx.x, + gridDim.x, ...): a
+// tile's offset, carried bytes and byte count are known before it starts, so
+// the next tile's lead codes and per-tile words are loaded at the start of an
+// iteration and its mid bytes copied with cp.async into the second staging
+// buffer while the current tile decodes.
 template <typename T>
-__global__ void __launch_bounds__(kNbThreads) k_nb_decode(const uint8_t* __restrict__ s, unsigned long long len,
-                                                          const NonBlockedHdr* hp,
-                                                          const unsigned long long* __restrict__ aux, T* out,
-                                                          unsigned long long* ctr) {
+constexpr int nb_dec_stage_bytes() { return ((kNbTile * (int)sizeof(T) + 48) + 15) / 16 * 16; }
+
+template <typename T>
+__global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
+    k_nb_decode(const uint8_t* __restrict__ s, unsigned long long len, const NonBlockedHdr* hp,
+                const uint32_t* __restrict__ tcnt, const unsigned long long* __restrict__ aux,
+                const unsigned long long* __restrict__ gsum, T* out) {
+    constexpr int kTpg = kNbThreads / 32;
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
     constexpr int TOPSH = 8 * (W - 3);
-    __shared__ __align__(16) uint8_t stage[kNbTile * W + 48];
+    extern __shared__ __align__(16) uint8_t nb_dyn[];   // two staging buffers of nb_dec_stage_bytes<T>()
     __shared__ uint32_t s_sum[8];
     __shared__ uint32_t s_wsum[8];
-    __shared__ long long s_tile;
     const NonBlockedHdr h = *hp;
     if (!h.ok) return;
     int R, sft;
     split_reqlen(h.reqLength, &R, &sft);
     if (R > W) return;
-    const unsigned long long ntiles = (h.n + kNbTile - 1) / kNbTile;
+    const long long ntiles = (long long)((h.n + kNbTile - 1) / kNbTile);
+    long long tile = blockIdx.x;
+    if (tile >= ntiles) return;
     const uint8_t* lead = s + 17;
     const uint8_t* mid = s + h.mid_off;
     const uint8_t* send = s + len;
     const T med = widen_median<T>(h.median);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(ctr, 1ull);
-        __syncthreads();
-        const long long tile = s_tile;
-        if (tile >= (long long)ntiles) break;
+    auto stage = [&](int k) { return nb_dyn + (k & 1) * nb_dec_stage_bytes<T>(); };
+    // the tile's mid bytes [base, base + tot) into staging buffer k, 16-byte
+    // chunks by cp.async, a chunk at either end of the stream byte by byte
+    auto copy_in = [&](int k, unsigned long long base, uint32_t tot) {
+        const uint8_t* src = mid + base;
+        const uint32_t sh = (uint32_t)((uintptr_t)src & 15);
+        const uint8_t* gbase = src - sh;
+        const uint32_t nch = (sh + tot + 15) >> 4;
+        uint8_t* stg = stage(k);
+        for (uint32_t c = threadIdx.x; c < nch; c += kNbThreads) {
+            const uint8_t* lo = gbase + (c << 4);
+            if (lo >= s && lo + 16 <= send) cp_async16(stg + (c << 4), lo);
+            else
+                for (int j = 0; j < 16; j++) stg[(c << 4) + j] = (lo + j >= s && lo + j < send) ? lo[j] : 0;
+        }
+        cp_async_commit();
+    };
+    // a tile's words: lead codes (per thread), group prefix + offset in the
+    // group, carried bytes, byte count
+    auto words = [&](long long t, uint32_t& cd, unsigned long long& ga, unsigned long long& la, uint32_t& cy,
+                     uint32_t& tot) {
+        cd = lead_word16(lead, (unsigned long long)t * kNbTile + threadIdx.x * kNbPer, h.L);
+        ga = gsum[t / kTpg];
+        la = aux[3 * t];
+        cy = (uint32_t)aux[3 * t + 1];
+        tot = tcnt[t];
+    };
+    const long long G = gridDim.x;
+    uint32_t cd0, cy0, tot0, cd1 = 0, cy1 = 0, tot1 = 0;
+    unsigned long long ga0, la0, ga1 = 0, la1 = 0;
+    words(tile, cd0, ga0, la0, cy0, tot0);
+    if (tile + G < ntiles) words(tile + G, cd1, ga1, la1, cy1, tot1);
+    copy_in(0, ga0 + la0, tot0);
+    const uint32_t full = R > 3 ? (uint32_t)(R - 3) : 0u;
+    for (int it = 0;; it++) {
+        const bool more = tile + G < ntiles;
+        // the words of the tile after next, in flight during this tile
+        uint32_t cd2 = 0, cy2 = 0, tot2 = 0;
+        unsigned long long ga2 = 0, la2 = 0;
+        if (tile + 2 * G < ntiles) words(tile + 2 * G, cd2, ga2, la2, cy2, tot2);
+        const uint32_t codes = cd0, carry = cy0;
+        const unsigned long long base = ga0 + la0;
         const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
-        const uint32_t codes = lead_word(lead, first >> 2, h.L);
-        int cnt[kNbPer];
-        uint32_t mine = 0;
-#pragma unroll
-        for (int e = 0; e < kNbPer; e++) {
-            int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
-            int c = R - ld;
-            cnt[e] = (first + e < h.n && c > 0) ? c : 0;
-            mine += cnt[e];
+        uint32_t mine;
+        {
+            const uint32_t valid = valid_pairs(first, h.n);
+            const uint32_t lo = codes & 0x55555555u, hi = (codes >> 1) & 0x55555555u;
+            mine = __popc(~(lo | hi) & valid) + (R >= 2 ? __popc(~hi & valid) : 0u) +
+                   (R >= 3 ? __popc(~(lo & hi) & valid) : 0u) + full * __popc(valid);
         }
         uint32_t total;
-        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);
-        const unsigned long long tbase = aux[3 * tile];
-        // carried bytes at the tile start: the latest earlier tile that stored each lane
-        uint32_t carry = 0;
-        {
-            const unsigned long long lw = aux[3 * tile + 1];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                unsigned long long t1 = (lw >> (21 * k)) & 0x1FFFFF;
-                if (t1) {
-                    unsigned long long u = t1 - 1;
-                    unsigned long long p1 = (aux[3 * u + 2] >> (21 * k)) & 0x1FFFFF;
-                    unsigned long long pos = h.mid_off + aux[3 * u] + (p1 - 1);
-                    uint32_t byte = pos < len ? s[pos] : 0u;
-                    carry |= byte << (8 * (2 - k));   // lane W-1-k sits at bits 8*(2-k) of the packed top bytes
-                }
-            }
-        }
-        // stage this tile's mid bytes
-        const uint8_t* src = mid + tbase;
-        cta_copy_in(stage, src, total, s, send);
-        __syncthreads();
-        const uint32_t sh = (uint32_t)((uintptr_t)src & 15);
-        const uint32_t* buf = (const uint32_t*)stage;
-        uint32_t q = sh + ex;
+        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // two barriers
+        if (more) copy_in(it + 1, ga1 + la1, tot1);
+        else cp_async_commit();   // an empty group: the wait below still means "this tile's copy"
+        cp_async_wait_group<1>();
+        __syncthreads();   // this tile's bytes are staged
+        const uint32_t* buf = (const uint32_t*)stage(it);
+        uint32_t q = (uint32_t)((uintptr_t)(mid + base) & 15) + ex;
         U sp[kNbPer];
-#pragma unroll
-        for (int e = 0; e < kNbPer; e++) {
-            uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
-            uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
-            if constexpr (sizeof(T) == 4) {
-                uint32_t m = cnt[e] >= 4 ? 0xFFFFFFFFu : ((1u << (8 * cnt[e])) - 1);
-                sp[e] = (lo & m) << (8 * (W - R));
-            } else {
-                uint32_t w2 = buf[(q >> 2) + 2];
-                uint32_t hi = __funnelshift_r(w1, w2, (q & 3) * 8);
-                unsigned long long v = ((unsigned long long)hi << 32) | lo;
-                unsigned long long m = cnt[e] >= 8 ? ~0ull : ((1ull << (8 * cnt[e])) - 1);
-                sp[e] = (v & m) << (8 * (W - R));
-            }
-            q += cnt[e];
-        }
-        // packed last-writer summary of the top three byte lanes (see blocked.cu)
+        // stored bytes, and the packed last-writer summary of the top three byte lanes
         uint32_t sv = 0, sm = 0;
 #pragma unroll
         for (int e = 0; e < kNbPer; e++) {
+            const int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+            const int c0 = R - ld;
+            const int c = (first + e < h.n && c0 > 0) ? c0 : 0;
+            const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
+            const uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
+            if constexpr (sizeof(T) == 4) {
+                const uint32_t m = c >= 4 ? 0xFFFFFFFFu : ((1u << (8 * c)) - 1);
+                sp[e] = (lo & m) << (8 * (W - R));
+            } else {
+                const uint32_t w2 = buf[(q >> 2) + 2];
+                const uint32_t hi = __funnelshift_r(w1, w2, (q & 3) * 8);
+                const unsigned long long v = ((unsigned long long)hi << 32) | lo;
+                const unsigned long long m = c >= 8 ? ~0ull : ((1ull << (8 * c)) - 1);
+                sp[e] = (v & m) << (8 * (W - R));
+            }
+            q += c;
             if (first + e < h.n) {
-                int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
-                uint32_t wm = (1u << (3 - ld)) - 1;
-                uint32_t wb = (wm & 1) * 0xFFu | (wm & 2) * 0x7F80u | (wm & 4) * 0x3FC000u;
-                uint32_t top = (uint32_t)(sp[e] >> TOPSH) & 0xFFFFFFu;
+                const uint32_t wm = (1u << (3 - ld)) - 1;
+                const uint32_t wb = (wm & 1) * 0xFFu | (wm & 2) * 0x7F80u | (wm & 4) * 0x3FC000u;
+                const uint32_t top = (uint32_t)(sp[e] >> TOPSH) & 0xFFFFFFu;
                 sv = (sv & ~wb) | (top & wb);
                 sm |= wm;
             }
         }
         auto comb = [](uint32_t A, uint32_t B) {
-            uint32_t bm = B >> 24;
-            uint32_t wb = (bm & 1) * 0xFFu | (bm & 2) * 0x7F80u | (bm & 4) * 0x3FC000u;
+            const uint32_t bm = B >> 24;
+            const uint32_t wb = (bm & 1) * 0xFFu | (bm & 2) * 0x7F80u | (bm & 4) * 0x3FC000u;
             return (((A >> 24) | bm) << 24) | ((A & 0xFFFFFFu & ~wb) | (B & 0xFFFFFFu & wb));
         };
         uint32_t sum = (sm << 24) | sv;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            uint32_t o = __shfl_up_sync(0xffffffffu, sum, d);
+            const uint32_t o = __shfl_up_sync(0xffffffffu, sum, d);
             if (lane >= d) sum = comb(o, sum);
         }
         if (lane == 31) s_wsum[warp] = sum;
         __syncthreads();
         uint32_t wpre = (7u << 24) | carry;
         for (int w = 0; w < warp; w++) wpre = comb(wpre, s_wsum[w]);
-        uint32_t exs = __shfl_up_sync(0xffffffffu, sum, 1);
-        uint32_t full = lane ? comb(wpre, exs) : wpre;
+        const uint32_t exs = __shfl_up_sync(0xffffffffu, sum, 1);
+        const uint32_t full = lane ? comb(wpre, exs) : wpre;
         U prev = (U)(full & 0xFFFFFFu) << TOPSH;
         T v[kNbPer];
         bool bad = false;
 #pragma unroll
         for (int e = 0; e < kNbPer; e++) {
-            int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
-            U inh = ld ? ~(((U)1 << (8 * (W - ld))) - 1) : (U)0;
-            U cur = sp[e] | (prev & inh);
+            const int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+            const U inh = ld ? ~(((U)1 << (8 * (W - ld))) - 1) : (U)0;
+            const U cur = sp[e] | (prev & inh);
             sp[e] = cur << sft;
             v[e] = EL::add(EL::of(sp[e]), med);
             bad |= v[e] != v[e];
@@ -660,8 +831,13 @@ __global__ void __launch_bounds__(kNbThreads) k_nb_decode(const uint8_t* __restr
             for (int e = 0; e < kNbPer; e++) v[e] = xadd(EL::of(sp[e]), med);
         }
         store16<T>(out, first, h.n, v);
-        __syncthreads();
+        if (!more) break;
+        __syncthreads();   // this tile's buffer and s_wsum are free again
+        tile += G;
+        cd0 = cd1; ga0 = ga1; la0 = la1; cy0 = cy1; tot0 = tot1;
+        cd1 = cd2; ga1 = ga2; la1 = la2; cy1 = cy2; tot1 = tot2;
     }
+    cp_async_wait_all();
 }
 
 cudaError_t launch_nonblocked_decode(int dtype, const uint8_t* d_stream, size_t len, size_t n, void* d_out,
@@ -670,31 +846,56 @@ cudaError_t launch_nonblocked_decode(int dtype, const uint8_t* d_stream, size_t 
     const size_t ntiles = (n + kNbTile - 1) / kNbTile;
     if (ntiles >= (1u << 21) - 1) return cudaErrorInvalidValue;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(ws.st32, 0, sizeof(uint32_t) * (ntiles + 8), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(ws.counters, 0, 2 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
+    uint32_t* tcnt = ws.st32;   // [ntiles] tile byte counts
+    const size_t ng = (ntiles + kNbThreads / 32 - 1) / (kNbThreads / 32);
+    unsigned long long* gsum = ws.st_word;                     // [ng] group byte totals, then prefixes
+    unsigned long long* gwr = ws.st_word + ws.status_tiles;    // [ng] group latest writers, then prefixes
     {
         TraceScope tr("nonblocked_parse", s);
         k_nb_parse<<<1, 1, 0, s>>>(d_stream, len, n, ws.nhdr, ws.err);
     }
-    size_t g = (size_t)sm_count() * 8;
-    int grid = (int)(ntiles < g ? ntiles : g);
-    TileStatus32 st{ws.st32, ws.st_agg2, ws.st_inc2};
     {
-        TraceScope tr("nonblocked_summary", s);
-        if (dtype == 0)
-            k_nb_summary<float><<<grid, kNbThreads, 0, s>>>(d_stream, ws.nhdr, ws.tile_aux, st, &ws.counters[0], ws.err);
-        else
-            k_nb_summary<double><<<grid, kNbThreads, 0, s>>>(d_stream, ws.nhdr, ws.tile_aux, st, &ws.counters[0],
-                                                             ws.err);
+        TraceScope tr("nonblocked_count", s);
+        if (dtype == 0) k_nb_count<float><<<(int)ng, kNbThreads, 0, s>>>(d_stream, ws.nhdr, tcnt, ws.tile_aux, gsum, gwr);
+        else k_nb_count<double><<<(int)ng, kNbThreads, 0, s>>>(d_stream, ws.nhdr, tcnt, ws.tile_aux, gsum, gwr);
     }
+    {
+        TraceScope tr("nonblocked_scan", s);
+        k_nb_scan<<<1, kScanThreads, 0, s>>>(ws.nhdr, gsum, gwr, ws.err);
+    }
+    {
+        TraceScope tr("nonblocked_carry", s);
+        k_nb_carry<<<(int)((ntiles + 255) / 256), 256, 0, s>>>(d_stream, len, ws.nhdr, ws.tile_aux, gsum, gwr);
+    }
+    static int per_sm[2][64] = {{0}};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    int& occ = per_sm[dtype == 0 ? 0 : 1][dev];
+    const size_t dyn = 2 * (size_t)(dtype == 0 ? nb_dec_stage_bytes<float>() : nb_dec_stage_bytes<double>());
+    if (!occ) {
+        if (dtype == 0) {
+            e = cudaFuncSetAttribute(k_nb_decode<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nb_decode<float>, kNbThreads, dyn);
+        } else {
+            e = cudaFuncSetAttribute(k_nb_decode<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nb_decode<double>, kNbThreads, dyn);
+        }
+        if (e != cudaSuccess) return e;
+        if (occ < 1) occ = 1;
+    }
+    const size_t g = (size_t)sm_count() * occ;
+    const int grid = (int)(ntiles < g ? ntiles : g);
     {
         TraceScope tr("nonblocked_decode", s);
         if (dtype == 0)
-            k_nb_decode<float><<<grid, kNbThreads, 0, s>>>(d_stream, len, ws.nhdr, ws.tile_aux, (float*)d_out,
-                                                           &ws.counters[1]);
+            k_nb_decode<float><<<grid, kNbThreads, dyn, s>>>(d_stream, len, ws.nhdr, tcnt, ws.tile_aux, gsum,
+                                                             (float*)d_out);
         else
-            k_nb_decode<double><<<grid, kNbThreads, 0, s>>>(d_stream, len, ws.nhdr, ws.tile_aux, (double*)d_out,
-                                                            &ws.counters[1]);
+            k_nb_decode<double><<<grid, kNbThreads, dyn, s>>>(d_stream, len, ws.nhdr, tcnt, ws.tile_aux, gsum,
+                                                              (double*)d_out);
     }
     return cudaGetLastError();
 }
