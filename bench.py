@@ -58,6 +58,9 @@ WORKLOADS = {
                      "(profiling size: 216 MiB, above L2)"),
     "c2m1": dict(shape=(512, 512, 512), mode=1, bs=128, rel=1e-3,
                  desc="512^3 float32 k^-5/3 Gaussian random field + 5% zero slabs, REL 1e-3, fastMode 1"),
+    "c2sm1": dict(shape=(384, 384, 384), mode=1, bs=128, rel=1e-3,
+                  desc="384^3 float32 k^-5/3 Gaussian random field + 5% zero slabs, REL 1e-3, fastMode 1 "
+                       "(profiling size: 216 MiB, above L2)"),
     "c5": dict(mode=2, bs=128,
                desc="learned fixed rate: 500 float32 fields, sizes log-uniform 2^20..2^26, seeded mix of spectral / "
                     "piecewise-constant (+1e-3 noise) / white noise, targets 8, 16, 32 within 5%, fastMode-2 "
@@ -414,11 +417,16 @@ def run_ours(args, wl, rank, world, local_rank):
     import oracle as O
     got = sv.cpu().numpy()
     threads = os.cpu_count() or 1
-    want, wlen = O.compress_m3_omp(xh, np.float32(eb), bs, threads=threads) if mode == 3 else (None, 0)
-    stream_equal = bool(mode == 3 and wlen == size and np.array_equal(got, want[:wlen]))
+    if mode == 3:
+        want, wlen = O.compress_m3_omp(xh, np.float32(eb), bs, threads=threads)
+    else:   # the serial oracle for the other layouts
+        want = np.frombuffer(O.fast_compress_args(mode, xh, REL, 0.0, rel, bs), np.uint8)
+        wlen = want.size
+    stream_equal = bool(wlen == size and np.array_equal(got, want[:wlen]))
     decode_equal = bool(stream_equal and np.array_equal(
         y.cpu().numpy().view(np.uint32),
-        O.decompress_m3_omp(np.float32, want, wlen, n, threads=threads).view(np.uint32)))
+        (O.decompress_m3_omp(np.float32, want, wlen, n, threads=threads) if mode == 3
+         else O.decompress(mode, np.float32, want.tobytes(), n)).view(np.uint32)))
     del want, got
     del codec, y
     torch.cuda.empty_cache()

@@ -752,12 +752,14 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
         const uint32_t codes = cd0, carry = cy0;
         const unsigned long long base = ga0 + la0;
         const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
-        uint32_t mine;
+        // lanes written by this thread's values: lane W-1-k by a value with lead <= k
+        uint32_t mine, sm;
         {
             const uint32_t valid = valid_pairs(first, h.n);
             const uint32_t lo = codes & 0x55555555u, hi = (codes >> 1) & 0x55555555u;
-            mine = __popc(~(lo | hi) & valid) + (R >= 2 ? __popc(~hi & valid) : 0u) +
-                   (R >= 3 ? __popc(~(lo & hi) & valid) : 0u) + full * __popc(valid);
+            const uint32_t m0 = ~(lo | hi) & valid, m1 = ~hi & valid, m2 = ~(lo & hi) & valid;
+            mine = __popc(m0) + (R >= 2 ? __popc(m1) : 0u) + (R >= 3 ? __popc(m2) : 0u) + full * __popc(valid);
+            sm = (m2 ? 1u : 0u) | (m1 ? 2u : 0u) | (m0 ? 4u : 0u);
         }
         uint32_t total;
         const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // two barriers
@@ -767,19 +769,20 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
         __syncthreads();   // this tile's bytes are staged
         const uint32_t* buf = (const uint32_t*)stage(it);
         uint32_t q = (uint32_t)((uintptr_t)(mid + base) & 15) + ex;
+        // Values past the end of the field (codes 0) are decoded like the
+        // others and never stored: they follow every real value, so nothing
+        // they change reaches one.
         U sp[kNbPer];
-        // stored bytes, and the packed last-writer summary of the top three byte lanes
-        uint32_t sv = 0, sm = 0;
+        U prev0 = 0;   // the thread's chain from an all-zero start: its top bytes summarise the thread
 #pragma unroll
         for (int e = 0; e < kNbPer; e++) {
-            const int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
-            const int c0 = R - ld;
-            const int c = (first + e < h.n && c0 > 0) ? c0 : 0;
+            const uint32_t ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+            const int c0 = R - (int)ld;
+            const uint32_t c = c0 > 0 ? (uint32_t)c0 : 0u;
             const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
             const uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
             if constexpr (sizeof(T) == 4) {
-                const uint32_t m = c >= 4 ? 0xFFFFFFFFu : ((1u << (8 * c)) - 1);
-                sp[e] = (lo & m) << (8 * (W - R));
+                sp[e] = (lo & __funnelshift_lc(0xFFFFFFFFu, 0u, 8 * c)) << (8 * (W - R));   // low c bytes (c <= 4)
             } else {
                 const uint32_t w2 = buf[(q >> 2) + 2];
                 const uint32_t hi = __funnelshift_r(w1, w2, (q & 3) * 8);
@@ -788,20 +791,15 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
                 sp[e] = (v & m) << (8 * (W - R));
             }
             q += c;
-            if (first + e < h.n) {
-                const uint32_t wm = (1u << (3 - ld)) - 1;
-                const uint32_t wb = (wm & 1) * 0xFFu | (wm & 2) * 0x7F80u | (wm & 4) * 0x3FC000u;
-                const uint32_t top = (uint32_t)(sp[e] >> TOPSH) & 0xFFFFFFu;
-                sv = (sv & ~wb) | (top & wb);
-                sm |= wm;
-            }
+            const U inh = ~((~(U)0) >> (8 * ld));   // the top `ld` bytes come from the previous value
+            prev0 = sp[e] | (prev0 & inh);
         }
         auto comb = [](uint32_t A, uint32_t B) {
             const uint32_t bm = B >> 24;
             const uint32_t wb = (bm & 1) * 0xFFu | (bm & 2) * 0x7F80u | (bm & 4) * 0x3FC000u;
             return (((A >> 24) | bm) << 24) | ((A & 0xFFFFFFu & ~wb) | (B & 0xFFFFFFu & wb));
         };
-        uint32_t sum = (sm << 24) | sv;
+        uint32_t sum = (sm << 24) | ((uint32_t)(prev0 >> TOPSH) & 0xFFFFFFu);
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const uint32_t o = __shfl_up_sync(0xffffffffu, sum, d);
@@ -812,14 +810,14 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
         uint32_t wpre = (7u << 24) | carry;
         for (int w = 0; w < warp; w++) wpre = comb(wpre, s_wsum[w]);
         const uint32_t exs = __shfl_up_sync(0xffffffffu, sum, 1);
-        const uint32_t full = lane ? comb(wpre, exs) : wpre;
-        U prev = (U)(full & 0xFFFFFFu) << TOPSH;
+        const uint32_t fullp = lane ? comb(wpre, exs) : wpre;
+        U prev = (U)(fullp & 0xFFFFFFu) << TOPSH;
         T v[kNbPer];
         bool bad = false;
 #pragma unroll
         for (int e = 0; e < kNbPer; e++) {
-            const int ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
-            const U inh = ld ? ~(((U)1 << (8 * (W - ld))) - 1) : (U)0;
+            const uint32_t ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
+            const U inh = ~((~(U)0) >> (8 * ld));
             const U cur = sp[e] | (prev & inh);
             sp[e] = cur << sft;
             v[e] = EL::add(EL::of(sp[e]), med);
