@@ -194,6 +194,17 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encod
     unsigned long long an_incl = 0;
     long long w_lo = 0;
     int w_ok = 0;
+    long long pend_t = -1;   // a tile placed from the window, its inclusive prefix not yet published
+    uint32_t pend_agg = 0;
+    auto publish = [&]() {
+        if (pend_t > 0 && lane == 0) {
+            __stcg(&a.st.inc_a[pend_t], an_incl);
+            __stcg(&a.st.inc_b[pend_t], 0ull);
+            __threadfence();
+            st_volatile32(&a.st.st[pend_t], kSt32Inc | (pend_agg & 0x7FFFFFu));
+        }
+        pend_t = -1;
+    };
     // warp 0: copy the status words of the tiles between the anchor and t
     auto win_issue = [&](long long t) {
         w_ok = 0;
@@ -240,11 +251,9 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encod
         if (!placed) {
             unsigned long long dummy;
             lookback_resolve(a.st, t, agg, 0, &base, &dummy, a.err);   // publishes t's inclusive prefix
-        } else if (t > 0 && lane == 0) {
-            __stcg(&a.st.inc_a[t], base + agg);
-            __stcg(&a.st.inc_b[t], 0ull);
-            __threadfence();
-            st_volatile32(&a.st.st[t], kSt32Inc | (agg & 0x7FFFFFu));
+        } else if (t > 0) {
+            pend_t = t;   // published after the barrier, off the CTA's critical path
+            pend_agg = agg;
         }
         an_t = t;
         an_incl = base + agg;
@@ -286,8 +295,6 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encod
     for (; tile < nt; it++) {
         // the next tile, claimed now and read after the scan's barriers
         if (threadIdx.x == 0) s_tile[(it + 1) & 1] = (long long)atomicAdd(a.tile_ctr, 1ull);
-        // T_{j-1}'s window, in flight during this tile's work
-        if (threadIdx.x < 32 && t1 >= 0) win_issue(t1);
         const unsigned long long first = (unsigned long long)tile * kNbTile + threadIdx.x * kNbPer;
         U cur[kNbPer];
         bool bad = false;
@@ -331,6 +338,8 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encod
         const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // two barriers
         if (threadIdx.x < 32) lookback_publish(a.st, tile, total, 0);
         if (threadIdx.x == 0) s_total[it & 1] = total;
+        // T_{j-1}'s window, in flight during the emission
+        if (threadIdx.x < 32 && t1 >= 0) win_issue(t1);
         // lead codes: 4 bytes per thread, at their fixed place
         const unsigned long long lb = first >> 2;
         if (lb + 4 <= L && ((uintptr_t)(lead + lb) & 3) == 0) *(uint32_t*)(lead + lb) = codes;
@@ -358,6 +367,7 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encod
         if (next < nt) fetch(next);
         if (threadIdx.x < 32 && t1 >= 0) place(t1, s_total[(it - 1) & 1]);
         __syncthreads();   // T_j staged; T_{j-1}'s offset known
+        if (threadIdx.x < 32) publish();
         if (t1 >= 0 && !s_skip) cta_copy_realign(stage(it - 1), s_total[(it - 1) & 1], mid + s_base);
         __syncthreads();   // T_{j-1}'s buffer and s_base are free again
         t1 = tile;
@@ -370,6 +380,7 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encod
             place(t1, s_total[(it - 1) & 1]);
         }
         __syncthreads();
+        if (threadIdx.x < 32) publish();
         if (!s_skip) cta_copy_realign(stage(it - 1), s_total[(it - 1) & 1], mid + s_base);
     }
 }
