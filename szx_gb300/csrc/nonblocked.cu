@@ -27,7 +27,9 @@ constexpr int kNbPer = 16;                        // values per thread
 constexpr int kNbTile = kNbThreads * kNbPer;      // 4096 values per tile
 constexpr unsigned long long kNbShift = 15;
 
-// CTA-wide exclusive sum (256 threads), returns the total through *tot.
+// CTA-wide exclusive sum (256 threads), returns the total through *tot.  One
+// barrier: the caller places another barrier between this call and the next
+// one that writes `sm`.
 __device__ __forceinline__ uint32_t cta_excl_sum32(uint32_t v, uint32_t* tot, uint32_t* sm /*[8]*/) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t incl = warp_inclusive_sum(v);
@@ -40,7 +42,6 @@ __device__ __forceinline__ uint32_t cta_excl_sum32(uint32_t v, uint32_t* tot, ui
         pre += w < warp ? x : 0;
         t += x;
     }
-    __syncthreads();
     *tot = t;
     return pre + incl - v;
 }
@@ -159,7 +160,7 @@ template <typename T>
 constexpr int nb_stage_bytes() { return ((kNbTile * (int)sizeof(T) + 48) + 15) / 16 * 16; }
 
 template <typename T>
-__global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encode(NbEncArgs a) {
+__global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 4 : 2) k_nb_encode(NbEncArgs a) {
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encod
             mine += (c4 * 0x01010101u) >> 24;
         }
         uint32_t total;
-        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // two barriers
+        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // one barrier
         if (threadIdx.x < 32) lookback_publish(a.st, tile, total, 0);
         if (threadIdx.x == 0) s_total[it & 1] = total;
         // T_{j-1}'s window, in flight during the emission
@@ -369,12 +370,15 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2) k_nb_encod
         __syncthreads();   // T_j staged; T_{j-1}'s offset known
         if (threadIdx.x < 32) publish();
         if (t1 >= 0 && !s_skip) cta_copy_realign(stage(it - 1), s_total[(it - 1) & 1], mid + s_base);
-        __syncthreads();   // T_{j-1}'s buffer and s_base are free again
+        // no barrier here: the next writes of T_{j-1}'s buffer (T_{j+1}'s
+        // emission), of s_base / s_skip (its placement) and of s_sum / s_total
+        // all come after the next iteration's scan barrier
         t1 = tile;
         tile = next;
     }
     // the last tile of this CTA
     if (t1 >= 0) {
+        __syncthreads();   // the last copy-out has read s_base / s_skip
         if (threadIdx.x < 32) {
             win_issue(t1);
             place(t1, s_total[(it - 1) & 1]);
@@ -773,7 +777,7 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
             sm = (m2 ? 1u : 0u) | (m1 ? 2u : 0u) | (m0 ? 4u : 0u);
         }
         uint32_t total;
-        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // two barriers
+        const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // one barrier
         if (more) copy_in(it + 1, ga1 + la1, tot1);
         else cp_async_commit();   // an empty group: the wait below still means "this tile's copy"
         cp_async_wait_group<1>();
@@ -841,7 +845,9 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
         }
         store16<T>(out, first, h.n, v);
         if (!more) break;
-        __syncthreads();   // this tile's buffer and s_wsum are free again
+        // no barrier here: this tile's buffer is next written by the copy
+        // issued after the next iteration's scan barrier, s_wsum after the
+        // barrier that follows that copy
         tile += G;
         cd0 = cd1; ga0 = ga1; la0 = la1; cy0 = cy1; tot0 = tot1;
         cd1 = cd2; ga1 = ga2; la1 = la2; cy1 = cy2; tot1 = tot2;
