@@ -85,3 +85,29 @@ def test_full_size_double_streams_and_values(field, bs, eb):
         slack = 0.5 * np.spacing(np.abs(med[blk])).astype(np.float64)
         assert (np.abs(yh[off] - xh[off]) <= eb * (1 + 1e-12) + slack).all()
     del codec
+
+
+@pytest.mark.parametrize("eb", [1e-1, 1e-3])
+def test_full_size_double_fastmode1(field, eb):
+    """The same 2 GiB field through fastMode 1 (the non-blocked layout,
+    szx/src/szx_double.cc:1593-2011, decoded by szx/src/szxd_double.cc:
+    683-1114): 65,536 tiles of 4096 values, so every persistent CTA of the
+    encoder and of the decoder works through many tiles (claim-ahead,
+    window placement, both staging buffers, the two-ahead prefetch).  Stream
+    and values must equal the serial oracle's."""
+    import torch
+    from szx_gb300.api import DeviceCodec
+    xd, xh = field
+    n = xh.size
+    codec = DeviceCodec(1, np.float64, n, blockSize=128)
+    codec.compress(xd, 0, eb, 0.0)
+    s = codec.stream_bytes()
+    got = s.cpu().numpy().tobytes()
+    want = O.fast_compress_args(1, xh, 0, eb, 0.0, 128)
+    assert len(got) == len(want) and got == want, eb
+    y = codec.decompress(s, n)
+    torch.cuda.synchronize()
+    assert codec.status() == 0
+    ref = O.decompress(1, np.float64, want, n)
+    assert np.array_equal(y.cpu().numpy().view(np.uint64), ref.view(np.uint64)), eb
+    del codec
