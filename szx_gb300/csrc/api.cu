@@ -166,19 +166,48 @@ size_t bound_for(int mode, int dtype, size_t n, int bs) {
     return mode == kNonBlocked ? nonblocked_bound(dtype, n) : blocked_bound(mode, dtype, n, bs);
 }
 
-// Enqueue compress; result lands in ws.result (device).
+__global__ void k_ws_clear(ClearList c) {
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nthr = (size_t)gridDim.x * blockDim.x;
+    for (int r = 0; r < c.n; r++) {
+        uint32_t* p = (uint32_t*)c.p[r];
+        const size_t words = c.bytes[r] / 4;
+        for (size_t i = tid; i < words; i += nthr) p[i] = 0u;
+    }
+}
+
+cudaError_t launch_ws_clear(const ClearList& c, cudaStream_t s) {
+    size_t words = 0;
+    for (int r = 0; r < c.n; r++) {
+        if (((uintptr_t)c.p[r] & 3) || (c.bytes[r] & 3)) return cudaErrorInvalidValue;
+        words = words > c.bytes[r] / 4 ? words : c.bytes[r] / 4;
+    }
+    const size_t want = (words + 255) / 256, cap = (size_t)sm_count() * 4;
+    const int grid = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+    k_ws_clear<<<grid, 256, 0, s>>>(c);
+    return cudaGetLastError();
+}
+
+// Enqueue compress; result lands in ws.result (device).  One launch clears
+// what the passes expect zeroed (the value-range pass's ticket among it), so
+// the value-range pass and the encoder skip their own clears.
 static int enqueue_compress(int mode, int dtype, const void* d_x, size_t n, int bs, int err_mode, float abs_eb,
                             float rel, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s) {
     cudaError_t e;
     if (mode == kNonBlocked) {
-        if ((e = launch_range(dtype, d_x, n, err_mode, abs_eb, rel, ws, s)) != cudaSuccess) return cuda_fail(e);
-        if ((e = launch_nonblocked_encode(dtype, d_x, n, d_out, cap, ws, s)) != cudaSuccess) return cuda_fail(e);
+        if ((e = launch_ws_clear(nonblocked_enc_clear(ws, n), s)) != cudaSuccess) return cuda_fail(e);
+        if ((e = launch_range(dtype, d_x, n, err_mode, abs_eb, rel, ws, s, true)) != cudaSuccess) return cuda_fail(e);
+        if ((e = launch_nonblocked_encode(dtype, d_x, n, d_out, cap, ws, s, true)) != cudaSuccess)
+            return cuda_fail(e);
         return SZXG_OK;
     }
     bool use_params = err_mode == REL;
-    if (use_params && (e = launch_range(dtype, d_x, n, err_mode, abs_eb, rel, ws, s)) != cudaSuccess)
+    if (n == 0 || bs < 1) return cuda_fail(cudaErrorInvalidValue);
+    if ((e = launch_ws_clear(blocked_enc_clear(ws, (n + bs - 1) / bs), s)) != cudaSuccess) return cuda_fail(e);
+    if (use_params && (e = launch_range(dtype, d_x, n, err_mode, abs_eb, rel, ws, s, true)) != cudaSuccess)
         return cuda_fail(e);
-    if ((e = launch_blocked_encode(mode, dtype, d_x, n, bs, use_params, abs_eb, d_out, cap, ws, s)) != cudaSuccess)
+    if ((e = launch_blocked_encode(mode, dtype, d_x, n, bs, use_params, abs_eb, d_out, cap, ws, s, true)) !=
+        cudaSuccess)
         return cuda_fail(e);
     return SZXG_OK;
 }

@@ -867,8 +867,19 @@ cudaError_t launch_blocked_encode_fields(int layout, int dtype, int bs, int nf, 
     return cudaGetLastError();
 }
 
+ClearList blocked_enc_clear(const Workspace& ws, size_t nb) {
+    ClearList c{};
+    c.p[0] = ws.st_word;
+    c.bytes[0] = 8 * blocked_status_words(nb);
+    c.p[1] = ws.totals;
+    c.bytes[1] = kWsHeaderClear;
+    c.n = 2;
+    return c;
+}
+
 cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
-                                  float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s) {
+                                  float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s,
+                                  bool cleared) {
     if (n == 0 || bs < 1 || bs > 256) return cudaErrorInvalidValue;
     if (layout == kBlocked && bs > 255) return cudaErrorInvalidValue;
     const size_t nb = (n + bs - 1) / bs, sb = (nb + 7) / 8;
@@ -877,8 +888,7 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
     if (cap < qfix) return cudaErrorInvalidValue;
     cudaError_t e;
     // status words of both look-backs, then totals / result / error / counters
-    if ((e = cudaMemsetAsync(ws.st_word, 0, 8 * blocked_status_words(nb), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync((uint8_t*)ws.totals, 0, kWsHeaderClear, s)) != cudaSuccess) return e;
+    if (!cleared && (e = launch_ws_clear(blocked_enc_clear(ws, nb), s)) != cudaSuccess) return e;
     const size_t tb = (size_t)blocked_tile_blocks(dtype, bs, 0);
     BlkField F;
     F.x = x; F.n = n; F.nb = nb;
@@ -1787,9 +1797,17 @@ cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream
     if (bs < 1 || bs > 256 || n == 0) return cudaErrorInvalidValue;
     const bool m2 = layout == kBlocked;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(ws.counters, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(ws.st_word, 0, sizeof(unsigned long long) * ws.status_tiles, s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(ws.st2_word, 0, sizeof(unsigned long long) * ws.status2_tiles, s)) != cudaSuccess) return e;
+    {
+        ClearList c{};   // the index kernel's tile counter and both look-backs' status words
+        c.p[0] = ws.counters;
+        c.bytes[0] = sizeof(unsigned long long);
+        c.p[1] = ws.st_word;
+        c.bytes[1] = sizeof(unsigned long long) * ws.status_tiles;
+        c.p[2] = ws.st2_word;
+        c.bytes[2] = sizeof(unsigned long long) * ws.status2_tiles;
+        c.n = 3;
+        if ((e = launch_ws_clear(c, s)) != cudaSuccess) return e;
+    }
     {
         TraceScope tr("blocked_parse", s);
         if (m2) k_m2_parse<<<1, 1, 0, s>>>(d_stream, len, n, (unsigned long long)bs, ws.bhdr, ws.err);

@@ -195,15 +195,32 @@ Workspace ws_carve(void* base, int layout, int dtype, size_t n, int bs);
 
 // ------------------------------------------------------------------ launchers (return cudaError_t)
 
+// Zeroes up to four workspace regions (4-byte aligned, sizes multiples of 4
+// bytes) in one launch: the status words, totals and counters a codec pass
+// expects clear, instead of one memset per region.
+struct ClearList {
+    void* p[4];
+    size_t bytes[4];
+    int n;
+};
+cudaError_t launch_ws_clear(const ClearList& c, cudaStream_t s);
+
 // Global value range + derived bound; writes *params.  err_mode 0 = ABS, 1 = REL.
+// cleared: the caller has zeroed counters[3] (the CTA ticket) already.
 cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float abs_eb, float rel,
-                         const Workspace& ws, cudaStream_t s);
+                         const Workspace& ws, cudaStream_t s, bool cleared = false);
 
 // Blocked encode (layouts 2, 3, 4): stats + encode + placement + header assembly.
 // d_out must hold blocked_bound() bytes; the stream lands at d_out + result.offset.
 size_t blocked_bound(int layout, int dtype, size_t n, int bs);
+// cleared: the caller has zeroed blocked_enc_clear()'s regions already.
 cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
-                                  float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s);
+                                  float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s,
+                                  bool cleared = false);
+// The regions a blocked encode of nb blocks expects zeroed: both look-backs'
+// status words, then totals / result / error / counters (counters[3], the
+// value-range pass's ticket, among them).
+ClearList blocked_enc_clear(const Workspace& ws, size_t nb);
 // Blocks per encode tile for this type and block size (tile counts of a
 // field table), and the encode + assemble of nf fields in one launch each:
 // `one` when nf == 1, else the device table d_fields (ascending tile starts)
@@ -244,8 +261,12 @@ cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream
 
 // Non-blocked (layout 1) encode / decode.
 size_t nonblocked_bound(int dtype, size_t n);
+// cleared: the caller has zeroed nonblocked_enc_clear()'s regions already.
 cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t* d_out, size_t cap,
-                                     const Workspace& ws, cudaStream_t s);
+                                     const Workspace& ws, cudaStream_t s, bool cleared = false);
+// The regions a non-blocked encode of n values expects zeroed: its tile
+// status words, then totals / result / error / counters.
+ClearList nonblocked_enc_clear(const Workspace& ws, size_t n);
 cudaError_t launch_nonblocked_decode(int dtype, const uint8_t* d_stream, size_t len, size_t n, void* d_out,
                                      const Workspace& ws, cudaStream_t s);
 

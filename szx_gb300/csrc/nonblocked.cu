@@ -394,14 +394,23 @@ size_t nonblocked_bound(int dtype, size_t n) {
     return kNbShift + 17 + (n + 3) / 4 + es * n + 64;
 }
 
+ClearList nonblocked_enc_clear(const Workspace& ws, size_t n) {
+    const size_t ntiles = (n + kNbTile - 1) / kNbTile;
+    ClearList c{};
+    c.p[0] = ws.st32;
+    c.bytes[0] = sizeof(uint32_t) * (ntiles + 8);
+    c.p[1] = ws.totals;
+    c.bytes[1] = kWsHeaderClear;
+    c.n = 2;
+    return c;
+}
+
 cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t* d_out, size_t cap,
-                                     const Workspace& ws, cudaStream_t s) {
+                                     const Workspace& ws, cudaStream_t s, bool cleared) {
     if (n == 0 || cap < nonblocked_bound(dtype, n) - 64) return cudaErrorInvalidValue;
     const size_t ntiles = (n + kNbTile - 1) / kNbTile;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(ws.st32, 0, sizeof(uint32_t) * (ntiles + 8), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(ws.counters, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(ws.err, 0, sizeof(int), s)) != cudaSuccess) return e;
+    if (!cleared && (e = launch_ws_clear(nonblocked_enc_clear(ws, n), s)) != cudaSuccess) return e;
     NbEncArgs a;
     a.x = x; a.n = n; a.ntiles = ntiles; a.cap = cap; a.params = ws.params; a.out = d_out;
     a.st = TileStatus32{ws.st32, ws.st_agg2, ws.st_inc2};

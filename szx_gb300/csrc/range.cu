@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kRangeThreads) k_range(const T* __restrict__ x
 constexpr size_t kStreamBytes = size_t(96) << 20;
 
 cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float abs_eb, float rel,
-                         const Workspace& ws, cudaStream_t s) {
+                         const Workspace& ws, cudaStream_t s, bool cleared) {
     if (n == 0) return cudaErrorInvalidValue;
     size_t es = dtype == 0 ? 4 : 8;
     size_t per_cta = (size_t)kRangeThreads * (64 / es) * 4;  // ~64 B per thread per round, 4 rounds
@@ -236,7 +236,7 @@ cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float
     int grid = (int)(want < cap ? (want ? want : 1) : cap);
     if (grid > 4096) grid = 4096;
     RangePartial* parts = reinterpret_cast<RangePartial*>(ws.partials);
-    cudaError_t e = cudaMemsetAsync(&ws.counters[3], 0, sizeof(unsigned long long), s);
+    cudaError_t e = cleared ? cudaSuccess : cudaMemsetAsync(&ws.counters[3], 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     const bool stream = n * es > kStreamBytes;
     TraceScope tr("range", s);
