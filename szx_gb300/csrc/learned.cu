@@ -1120,7 +1120,10 @@ int SZxG_batch_features(SZxG_Batch* b, int nRows, const int* fieldOfRow, const f
 //   that double away from the measured side (as the reference's search
 //   brackets before it bisects) and bisected.
 // Both stop when a measured bracket is narrower than 2^-10 in y (the ratio
-// jumps over the target band there).  At most maxPasses passes per field,
+// jumps over the target band there).  The bound's exponent sets every
+// block's reqLength, so the ratio steps at each power of two P of the bound:
+// a bracket whose ends hold exactly one P between them probes P and the float
+// just below it, and ends when both lie on opposite sides of the band.  At most maxPasses passes per field,
 // plus one for a field that stopped unconverged after a pass that was not its
 // best.
 int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targetRatio, float tolerance,
@@ -1180,7 +1183,27 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
     // band (a smaller correction cannot change the outcome much)
     std::vector<double> ys(nf, 0.0);
     std::vector<float> aim = tgt;   // the target each field's sampled crossing was last taken for
+    // the first crossing's feature rows (field order): a crossing for another
+    // aim that falls inside a row's 1/64-step window is read off its curve
+    // (the same probe bounds, the same linear step) instead of probed again
+    std::vector<float> Xh;
+    auto window_crossing = [&](int f, float a, double& yout) {
+        const float* r = Xh.data() + (size_t)f * kF;
+        const double v = log2((double)a) - (double)r[0];   // the aim relative to the row's target
+        const float* u = r + 13;
+        for (int j = 0; j + 1 < kFine; j++)
+            if ((double)u[j] < v && v <= (double)u[j + 1]) {
+                yout = (double)r[4] + (j + (v - u[j]) / ((double)u[j + 1] - u[j])) / 64.0;
+                return true;
+            }
+        return false;
+    };
     if (mlp && e == cudaSuccess) e = crossing(all, tgt, ys, true);
+    if (mlp && e == cudaSuccess) {
+        Xh.resize((size_t)nf * kF);
+        e = cudaMemcpyAsync(Xh.data(), b->lfx->X, sizeof(float) * kF * nf, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
     if (mlp && e == cudaSuccess) e = predict_miss(pred);
     if (mlp && e == cudaSuccess) {
         std::vector<int> moved;
@@ -1189,7 +1212,9 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
             const double mu = std::min(std::max((double)pred[f], -1.0), 1.0);
             if (fabs(mu) >= quarter_band) {
                 aim[f] = (float)((double)tgt[f] * exp2(-mu));
-                moved.push_back(f);
+                double yw;
+                if (window_crossing(f, aim[f], yw)) ys[f] = yw;
+                else moved.push_back(f);
             }
         }
         e = crossing(moved, aim, ys, false);
@@ -1203,6 +1228,21 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
     std::vector<int> passes(nf, 0), done(nf, 0), stage(nf, 0), last_is_best(nf, 0), lo_m(nf, 0), hi_m(nf, 0);
     std::vector<float> ebk(nf);
     for (int f = 0; f < nf; f++) ebk[f] = b->tab[f].eb;
+    // bounds of the bracket's measured ends, of the best pass, and a bound
+    // to code exactly in the next pass (0: from y)
+    std::vector<float> lo_eb(nf, 0.f), hi_eb(nf, 0.f), best_eb(nf, 0.f), ebx(nf, 0.f);
+    // one power of two P between the bracket's ends: the side of P to code
+    // next, -1 when both sides are measured (the ratio jumps over the band
+    // at P), 0 when the ends hold none or several
+    auto jump_probe = [](float le, float he) -> float {
+        int xl, xh;
+        frexpf(le, &xl);
+        frexpf(he, &xh);
+        if (xh != xl + 1) return 0.f;
+        const float P = ldexpf(1.f, xh - 1), Pm = nextafterf(P, 0.f);
+        if (le == Pm && he == P) return -1.f;
+        return he > P ? P : Pm;
+    };
     std::vector<StreamResult> res(nf);
     auto eb_of = [&](int f, double yy) {
         const float r = range[f] > 0.f ? range[f] : 1.f;
@@ -1223,7 +1263,8 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
         for (int f = 0; f < nf; f++)
             if (!done[f]) {
                 act.push_back(f);
-                ebs.push_back(eb_of(f, y[f]));
+                ebs.push_back(ebx[f] > 0.f ? ebx[f] : eb_of(f, y[f]));
+                ebx[f] = 0.f;
             }
         if (act.empty()) break;
         e = batch_select(b, (int)act.size(), act.data(), ebs.data(), s);
@@ -1248,12 +1289,20 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
             if (rel < best_err[f]) {
                 best_err[f] = rel;
                 best_y[f] = y[f];
+                best_eb[f] = ebs[k];
                 best_cr[f] = cr;
                 last_is_best[f] = 1;
             }
             if (rel <= tolerance) { done[f] = 1; continue; }
-            if (cr < tgt[f]) { lo[f] = std::max(lo[f], y[f]); lo_m[f] = 1; }
-            else { hi[f] = std::min(hi[f], y[f]); hi_m[f] = 1; }
+            if (cr < tgt[f]) {
+                if (!lo_m[f] || ebs[k] > lo_eb[f]) lo_eb[f] = ebs[k];
+                lo[f] = std::max(lo[f], y[f]);
+                lo_m[f] = 1;
+            } else {
+                if (!hi_m[f] || ebs[k] < hi_eb[f]) hi_eb[f] = ebs[k];
+                hi[f] = std::min(hi[f], y[f]);
+                hi_m[f] = 1;
+            }
             // the ratio jumps over the target band inside a bracket this narrow: nothing to find
             if (lo_m[f] && hi_m[f] && hi[f] - lo[f] < kBracketStop) { done[f] = 2; continue; }
             const double ycur = y[f];
@@ -1263,19 +1312,33 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
                 t2[f] = (float)((double)aim[f] * std::min(std::max((double)tgt[f] / cr, 0.25), 4.0));
                 need_refine = true;
             } else {
-                y[f] = next_y(f);
+                const float pr = lo_m[f] && hi_m[f] ? jump_probe(lo_eb[f], hi_eb[f]) : 0.f;
+                if (pr < 0.f) { done[f] = 2; continue; }
+                if (pr > 0.f) {
+                    ebx[f] = pr;
+                    y[f] = log2((double)pr / (double)(range[f] > 0.f ? range[f] : 1.f));
+                } else {
+                    y[f] = next_y(f);
+                }
             }
             yprev[f] = ycur;
         }
         if (err_code) break;
         if (need_refine) {
-            std::vector<int> fl;
+            std::vector<int> fl, fw;
             for (int f = 0; f < nf; f++)
                 if (!done[f] && stage[f] == 1) {
                     if (!(t2[f] > 0.f) || !std::isfinite(t2[f])) t2[f] = aim[f];
-                    fl.push_back(f);
+                    double yw;
+                    if (window_crossing(f, t2[f], yw)) {
+                        ys[f] = yw;
+                        fw.push_back(f);
+                    } else {
+                        fl.push_back(f);
+                    }
                 }
             if ((e = crossing(fl, t2, ys, false)) != cudaSuccess) return fail_code(e);
+            fl.insert(fl.end(), fw.begin(), fw.end());
             for (int f : fl) {
                 stage[f] = 2;
                 y[f] = (ys[f] > lo[f] && ys[f] < hi[f]) ? ys[f] : next_y(f);
@@ -1289,7 +1352,7 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
         for (int f = 0; f < nf; f++)
             if (done[f] != 1 && !last_is_best[f] && best_err[f] < 1e300) {
                 act.push_back(f);
-                ebs.push_back(eb_of(f, best_y[f]));
+                ebs.push_back(best_eb[f]);
                 passes[f]++;
                 ebk[f] = ebs.back();
             }
