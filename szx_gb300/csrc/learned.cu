@@ -1120,10 +1120,11 @@ int SZxG_batch_features(SZxG_Batch* b, int nRows, const int* fieldOfRow, const f
 //   that double away from the measured side (as the reference's search
 //   brackets before it bisects) and bisected.
 // Both stop when a measured bracket is narrower than 2^-10 in y (the ratio
-// jumps over the target band there).  The bound's exponent sets every
-// block's reqLength, so the ratio steps at each power of two P of the bound:
-// a bracket whose ends hold exactly one P between them probes P and the float
-// just below it, and ends when both lie on opposite sides of the band.  At most maxPasses passes per field,
+// jumps over the target band there).  With a network: the bound's exponent
+// sets every block's reqLength, so the ratio steps at each power of two P of
+// the bound; a bracket whose ends hold exactly one P between them probes P
+// and the float just below it, and ends when both lie on opposite sides of
+// the band.  Plain bisection stays plain.  At most maxPasses passes per field,
 // plus one for a field that stopped unconverged after a pass that was not its
 // best.
 int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targetRatio, float tolerance,
@@ -1312,7 +1313,7 @@ int SZxG_batch_fixed_rate(SZxG_Batch* b, const SZxG_Mlp* mlp, const float* targe
                 t2[f] = (float)((double)aim[f] * std::min(std::max((double)tgt[f] / cr, 0.25), 4.0));
                 need_refine = true;
             } else {
-                const float pr = lo_m[f] && hi_m[f] ? jump_probe(lo_eb[f], hi_eb[f]) : 0.f;
+                const float pr = mlp && lo_m[f] && hi_m[f] ? jump_probe(lo_eb[f], hi_eb[f]) : 0.f;
                 if (pr < 0.f) { done[f] = 2; continue; }
                 if (pr > 0.f) {
                     ebx[f] = pr;
