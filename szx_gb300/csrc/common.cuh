@@ -380,21 +380,6 @@ struct SumPolicy {
     static __device__ __forceinline__ unsigned long long op(unsigned long long x, unsigned long long y) { return x + y; }
     static __device__ __forceinline__ unsigned long long reduce(unsigned long long v) { return warp_sum(v); }
 };
-// WriterPolicy: the field's three bits say which of the top three byte lanes
-// the tile stored; the prefix is, per lane, the latest such tile (+1, 21 bits
-// each, 0 = none), combined by max.
-struct WriterPolicy {
-    static __device__ __forceinline__ unsigned long long contrib(uint32_t f, long long u) {
-        unsigned long long t = (unsigned long long)(u + 1);
-        return ((f & 1) ? t : 0ull) | ((f & 2) ? t << 21 : 0ull) | ((f & 4) ? t << 42 : 0ull);
-    }
-    static __device__ __forceinline__ unsigned long long op(unsigned long long x, unsigned long long y) {
-        return Max3x21Op::op(x, y);
-    }
-    static __device__ __forceinline__ unsigned long long reduce(unsigned long long v) {
-        return Max3x21Op::warp_reduce(v);
-    }
-};
 
 // Whole warp.  agg_a < 2^23 (a sum), agg_b < 128 (combined by Policy).
 // Returns the exclusive prefixes.

@@ -9,11 +9,13 @@
 // One global median/radius (from the value-range pass) and ONE XOR chain over
 // the whole array: each value's lead code depends only on its predecessor, so
 // codes are data-parallel; mid-byte positions need a device-wide prefix sum
-// (decoupled look-back over 4096-value tiles).  Decoding must also find, for
-// every value, the last earlier value that stored each of the top three byte
-// lanes -- possibly many tiles back -- which a per-tile look-back of
-// "latest writer tile" indices (packed max) resolves in the same pass that
-// places the tiles' mid bytes.
+// (encoder: decoupled look-back over 4096-value tiles, placed from the CTA's
+// own previous tile and a window of status words).  Decoding must also find,
+// for every value, the last earlier value that stored each of the top three
+// byte lanes -- possibly many tiles back.  The lead codes alone give every
+// tile's byte count and its last writers, so the decoder needs no look-back:
+// per-tile counts (k_nb_count), one scan of group totals (k_nb_scan), the
+// carried bytes per tile (k_nb_carry), then the tiles decode independently.
 //
 // The stream is placed 15 bytes into the output buffer so the lead-code array
 // (stream offset 17) starts 16-byte aligned.
