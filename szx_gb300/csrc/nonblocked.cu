@@ -166,12 +166,12 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 4 : 2) k_nb_encod
     using EL = Elem<T>;
     using U = typename EL::U;
     constexpr int W = EL::W;
-    extern __shared__ __align__(16) uint8_t nb_dyn[];   // two staging buffers of nb_stage_bytes<T>()
-    auto stage = [&](int k) { return nb_dyn + (k & 1) * nb_stage_bytes<T>(); };
+    extern __shared__ __align__(16) uint8_t nb_dyn[];   // three staging buffers of nb_stage_bytes<T>()
+    auto stage = [&](int k) { return nb_dyn + ((unsigned)k % 3u) * nb_stage_bytes<T>(); };
     __shared__ __align__(16) uint32_t s_win[kNbWin + 8];
     __shared__ uint32_t s_sum[8];
     __shared__ long long s_tile[2];
-    __shared__ uint32_t s_total[2];
+    __shared__ uint32_t s_total[3];
     __shared__ unsigned long long s_base;
     __shared__ int s_skip;
     const T* x = (const T*)a.x;
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 4 : 2) k_nb_encod
     if (threadIdx.x == 0) s_tile[0] = (long long)atomicAdd(a.tile_ctr, 1ull);
     __syncthreads();
     long long tile = s_tile[0];
-    long long t1 = -1;   // T_{j-1}, waiting for its placement
+    long long t1 = -1, t2 = -1;   // T_{j-1}, T_{j-2}: staged, T_{j-2} placed in this iteration
     T v[kNbPer];
     T before = (T)0;     // lane 0: the value before its first one
     auto fetch = [&](long long t) {
@@ -340,9 +340,9 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 4 : 2) k_nb_encod
         uint32_t total;
         const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // one barrier
         if (threadIdx.x < 32) lookback_publish(a.st, tile, total, 0);
-        if (threadIdx.x == 0) s_total[it & 1] = total;
-        // T_{j-1}'s window, in flight during the emission
-        if (threadIdx.x < 32 && t1 >= 0) win_issue(t1);
+        if (threadIdx.x == 0) s_total[it % 3] = total;
+        // T_{j-2}'s window, in flight during the emission
+        if (threadIdx.x < 32 && t2 >= 0) win_issue(t2);
         // lead codes: 4 bytes per thread, at their fixed place
         const unsigned long long lb = first >> 2;
         if (lb + 4 <= L && ((uintptr_t)(lead + lb) & 3) == 0) *(uint32_t*)(lead + lb) = codes;
@@ -368,26 +368,29 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 4 : 2) k_nb_encod
         // the next tile's values are in flight during the placement
         const long long next = s_tile[(it + 1) & 1];
         if (next < nt) fetch(next);
-        if (threadIdx.x < 32 && t1 >= 0) place(t1, s_total[(it - 1) & 1]);
-        __syncthreads();   // T_j staged; T_{j-1}'s offset known
+        if (threadIdx.x < 32 && t2 >= 0) place(t2, s_total[(it - 2) % 3]);
+        __syncthreads();   // T_j staged; T_{j-2}'s offset known
         if (threadIdx.x < 32) publish();
-        if (t1 >= 0 && !s_skip) cta_copy_realign(stage(it - 1), s_total[(it - 1) & 1], mid + s_base);
-        // no barrier here: the next writes of T_{j-1}'s buffer (T_{j+1}'s
-        // emission), of s_base / s_skip (its placement) and of s_sum / s_total
-        // all come after the next iteration's scan barrier
+        if (t2 >= 0 && !s_skip) cta_copy_realign(stage(it - 2), s_total[(it - 2) % 3], mid + s_base);
+        // no barrier here: the next writes of T_{j-2}'s buffer (T_{j+1}'s
+        // emission), of s_base / s_skip (the next placement) and of s_sum /
+        // s_total all come after the next iteration's scan barrier
+        t2 = t1;
         t1 = tile;
         tile = next;
     }
-    // the last tile of this CTA
-    if (t1 >= 0) {
+    // the CTA's last two tiles, oldest first
+    for (int back = 2; back >= 1; back--) {
+        const long long t = back == 2 ? t2 : t1;
+        if (t < 0) continue;
         __syncthreads();   // the last copy-out has read s_base / s_skip
         if (threadIdx.x < 32) {
-            win_issue(t1);
-            place(t1, s_total[(it - 1) & 1]);
+            win_issue(t);
+            place(t, s_total[(it - back) % 3]);
         }
         __syncthreads();
         if (threadIdx.x < 32) publish();
-        if (!s_skip) cta_copy_realign(stage(it - 1), s_total[(it - 1) & 1], mid + s_base);
+        if (!s_skip) cta_copy_realign(stage(it - back), s_total[(it - back) % 3], mid + s_base);
     }
 }
 
@@ -424,7 +427,7 @@ cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     int& occ = per_sm[dtype == 0 ? 0 : 1][dev];
-    const size_t dyn = 2 * (size_t)(dtype == 0 ? nb_stage_bytes<float>() : nb_stage_bytes<double>());
+    const size_t dyn = 3 * (size_t)(dtype == 0 ? nb_stage_bytes<float>() : nb_stage_bytes<double>());
     if (!occ) {
         if (dtype == 0) {
             e = cudaFuncSetAttribute(k_nb_encode<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
