@@ -135,7 +135,15 @@ __global__ void __launch_bounds__(kRangeThreads) k_range(const T* __restrict__ x
 #pragma unroll
             for (int u = 0; u < 8; u++) add_vec<T>(acc, a[u], (i + u * nthr) * VN);
         }
-        for (; i < nv; i += nthr) add_vec<T>(acc, xv[i], i * VN);
+        if (i < nv) {   // the last partial round: its loads in flight together too
+            V a[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (i + u * nthr < nv) a[u] = STREAM ? __ldcs(xv + i + u * nthr) : xv[i + u * nthr];
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (i + u * nthr < nv) add_vec<T>(acc, a[u], (i + u * nthr) * VN);
+        }
         for (unsigned long long j = nv * VN + tid; j < n; j += nthr) acc.add(x[j], j);
     } else {
         for (unsigned long long j = tid; j < n; j += nthr) acc.add(x[j], j);
@@ -232,13 +240,30 @@ cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float
     size_t es = dtype == 0 ? 4 : 8;
     size_t per_cta = (size_t)kRangeThreads * (64 / es) * 4;  // ~64 B per thread per round, 4 rounds
     size_t want = (n + per_cta - 1) / per_cta;
-    size_t cap = (size_t)sm_count() * 8;
+    // one wave of resident CTAs: a second, partial wave would leave most SMs idle at the end
+    static int per_sm[2][2][64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    const bool stream = n * es > kStreamBytes;
+    int& occ = per_sm[dtype == 0 ? 0 : 1][stream ? 1 : 0][dev];
+    if (!occ) {
+        cudaError_t eo;
+        if (dtype == 0)
+            eo = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &occ, stream ? k_range<float, true> : k_range<float, false>, kRangeThreads, 0);
+        else
+            eo = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &occ, stream ? k_range<double, true> : k_range<double, false>, kRangeThreads, 0);
+        if (eo != cudaSuccess) return eo;
+        if (occ < 1) occ = 1;
+    }
+    size_t cap = (size_t)sm_count() * occ;
     int grid = (int)(want < cap ? (want ? want : 1) : cap);
     if (grid > 4096) grid = 4096;
     RangePartial* parts = reinterpret_cast<RangePartial*>(ws.partials);
     cudaError_t e = cleared ? cudaSuccess : cudaMemsetAsync(&ws.counters[3], 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    const bool stream = n * es > kStreamBytes;
     TraceScope tr("range", s);
     if (dtype == 0)
         (stream ? k_range<float, true> : k_range<float, false>)<<<grid, kRangeThreads, 0, s>>>(
