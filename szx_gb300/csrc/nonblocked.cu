@@ -148,13 +148,15 @@ struct NbEncArgs {
 // thread's last, or the value before the tile), a CTA scan of the
 // stored-byte counts, the tile's byte count published to the look-back, the
 // lead codes written to their fixed place, the mid bytes emitted into one of
-// two shared staging buffers with byte stores at tile-local offsets.  T_{j-1}
-// is placed one iteration late: its offset is the inclusive prefix of this
-// CTA's previous tile (known here) plus the counts of the tiles claimed in
-// between, read from a window of status words copied in with cp.async at the
-// start of the iteration (a window with unpublished words is copied again a
-// few times, then the global look-back takes over); then the CTA copies
-// T_{j-1}'s bytes out, realigned.
+// three shared staging buffers with byte stores at tile-local offsets.
+// T_{j-2} is placed two iterations late, so that the other CTAs' tiles
+// claimed before it have normally published their counts: its offset is the
+// inclusive prefix of this CTA's previous tile (known here) plus the counts
+// of the tiles claimed in between, read from a window of status words copied
+// in with cp.async during the emission (a window with unpublished words is
+// copied again a few times, then the global look-back takes over); then the
+// CTA copies T_{j-2}'s bytes out, realigned.  Two barriers per tile: the
+// scan's and the one that hands the placement to the copy-out.
 constexpr int kNbWin = 1024;   // status words per placement window (4 KiB)
 constexpr int kNbRepolls = 32;
 
