@@ -200,8 +200,30 @@ def test_corrupt_and_truncated_streams_fail_cleanly(szx):
     s1 = szx.fast_compress_args(1, x, 0, 1e-3)
     with pytest.raises(szx.SZxError):
         szx.fast_decompress(1, np.float32, s1[: len(s1) - 1000], x.size)
+    with pytest.raises(szx.SZxError):   # shorter than the fastMode-1 header
+        szx.fast_decompress(1, np.float32, s1[:10], x.size)
+    for req in (0, 65):                  # reqLength outside 1..64
+        bad1 = bytearray(s1)
+        bad1[4] = req
+        with pytest.raises(szx.SZxError):
+            szx.fast_decompress(1, np.float32, bytes(bad1), x.size)
+    # a lead-code count that does not match the value count
+    bad1 = bytearray(s1)
+    bad1[9:17] = ((x.size + 3) // 4 + 1).to_bytes(8, "big")
+    with pytest.raises(szx.SZxError):
+        szx.fast_decompress(1, np.float32, bytes(bad1), x.size)
+    # lead codes scrambled: whatever the counts say, every read stays inside
+    # the stream (an error or some values, never a fault)
+    bad1 = bytearray(s1)
+    bad1[17:17 + 4096] = np.random.default_rng(5).integers(0, 256, 4096, dtype=np.uint8).tobytes()
+    try:
+        szx.fast_decompress(1, np.float32, bytes(bad1), x.size)
+    except szx.SZxError:
+        pass
     # the library still works afterwards
     assert szx.fast_compress_args(3, x, 0, 1e-3) == s
+    assert szx.fast_decompress(1, np.float32, s1, x.size).tobytes() == \
+        O.decompress(1, np.float32, s1, x.size).tobytes()
 
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
