@@ -726,7 +726,7 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
     constexpr int TOPSH = 8 * (W - 3);
     extern __shared__ __align__(16) uint8_t nb_dyn[];   // two staging buffers of nb_dec_stage_bytes<T>()
     __shared__ uint32_t s_sum[8];
-    __shared__ uint32_t s_wsum[8];
+    __shared__ uint32_t s_wv[8], s_wm[8];   // per warp: last written top bytes, their byte mask
     const NonBlockedHdr h = *hp;
     if (!h.ok) return;
     int R, sft;
@@ -790,7 +790,7 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
             const uint32_t lo = codes & 0x55555555u, hi = (codes >> 1) & 0x55555555u;
             const uint32_t m0 = ~(lo | hi) & valid, m1 = ~hi & valid, m2 = ~(lo & hi) & valid;
             mine = __popc(m0) + (R >= 2 ? __popc(m1) : 0u) + (R >= 3 ? __popc(m2) : 0u) + full * __popc(valid);
-            sm = (m2 ? 1u : 0u) | (m1 ? 2u : 0u) | (m0 ? 4u : 0u);
+            sm = (m2 ? 0xFFu : 0u) | (m1 ? 0xFF00u : 0u) | (m0 ? 0xFF0000u : 0u);
         }
         uint32_t total;
         const uint32_t ex = cta_excl_sum32(mine, &total, s_sum);   // one barrier
@@ -825,24 +825,30 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
             const U inh = ~((~(U)0) >> (8 * ld));   // the top `ld` bytes come from the previous value
             prev0 = sp[e] | (prev0 & inh);
         }
-        auto comb = [](uint32_t A, uint32_t B) {
-            const uint32_t bm = B >> 24;
-            const uint32_t wb = (bm & 1) * 0xFFu | (bm & 2) * 0x7F80u | (bm & 4) * 0x3FC000u;
-            return (((A >> 24) | bm) << 24) | ((A & 0xFFFFFFu & ~wb) | (B & 0xFFFFFFu & wb));
-        };
-        uint32_t sum = (sm << 24) | ((uint32_t)(prev0 >> TOPSH) & 0xFFFFFFu);
+        // (top bytes, byte mask) pairs: a later pair's masked bytes win,
+        // masks accumulate -- one three-input logic op each
+        uint32_t sv = (uint32_t)(prev0 >> TOPSH) & 0xFFFFFFu, sw = sm;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t o = __shfl_up_sync(0xffffffffu, sum, d);
-            if (lane >= d) sum = comb(o, sum);
+            const uint32_t ov = __shfl_up_sync(0xffffffffu, sv, d), ow = __shfl_up_sync(0xffffffffu, sw, d);
+            if (lane >= d) {
+                sv = (ov & ~sw) | (sv & sw);
+                sw |= ow;
+            }
         }
-        if (lane == 31) s_wsum[warp] = sum;
+        if (lane == 31) {
+            s_wv[warp] = sv;
+            s_wm[warp] = sw;
+        }
         __syncthreads();
-        uint32_t wpre = (7u << 24) | carry;
-        for (int w = 0; w < warp; w++) wpre = comb(wpre, s_wsum[w]);
-        const uint32_t exs = __shfl_up_sync(0xffffffffu, sum, 1);
-        const uint32_t fullp = lane ? comb(wpre, exs) : wpre;
-        U prev = (U)(fullp & 0xFFFFFFu) << TOPSH;
+        uint32_t pv = carry;   // the carried bytes: all three lanes written before the tile
+        for (int w = 0; w < warp; w++) {
+            const uint32_t m = s_wm[w];
+            pv = (pv & ~m) | (s_wv[w] & m);
+        }
+        const uint32_t ev = __shfl_up_sync(0xffffffffu, sv, 1), ew = __shfl_up_sync(0xffffffffu, sw, 1);
+        if (lane) pv = (pv & ~ew) | (ev & ew);
+        U prev = (U)pv << TOPSH;
         T v[kNbPer];
         bool bad = false;
 #pragma unroll
