@@ -1339,16 +1339,21 @@ __device__ __forceinline__ void dec_segment_seq(const uint8_t* p, int len, T* ob
             q += byte_of(cnt[k], i);
         }
     }
-    // lane summary: [25:24] smallest lead in the lane, [23:0] top three bytes of its last value
-    uint32_t inc = (mlead << 24) | ((uint32_t)(run >> TOPSH) & 0xFFFFFFu);
+    // lane summary: the top three bytes of its last value, scanned over the
+    // segment as (top three bytes, byte mask of the ones the lane wrote): a later
+    // lane's written bytes win; bytes no lane wrote stay zero (the chain of
+    // every lane starts at zero)
+    uint32_t sv = (uint32_t)(run >> TOPSH) & 0xFFFFFFu, sw = 0xFFFFFFu >> (8 * mlead);
 #pragma unroll
     for (int d = 1; d < G; d <<= 1) {
-        const uint32_t o = __shfl_up_sync(0xffffffffu, inc, d, G);
-        if (sl >= d) inc = lw_op(o, inc);
+        const uint32_t ov = __shfl_up_sync(0xffffffffu, sv, d, G), ow = __shfl_up_sync(0xffffffffu, sw, d, G);
+        if (sl >= d) {
+            sv = (ov & ~sw) | (sv & sw);
+            sw |= ow;
+        }
     }
-    uint32_t ex = __shfl_up_sync(0xffffffffu, inc, 1, G);
-    if (sl == 0) ex = kLwNone;
-    const uint32_t carry = (ex & 0xFFFFFFu) << 8;   // top three bytes of a 32-bit word
+    const uint32_t ex = __shfl_up_sync(0xffffffffu, sv, 1, G);
+    const uint32_t carry = sl ? ex << 8 : 0u;   // top three bytes of a 32-bit word
     const T med = widen_median<T>(__uint_as_float(mb));
     T v[E];
 #pragma unroll
