@@ -188,25 +188,32 @@ cudaError_t launch_ws_clear(const ClearList& c, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-// Enqueue compress; result lands in ws.result (device).  One launch clears
-// what the passes expect zeroed (the value-range pass's ticket among it), so
-// the value-range pass and the encoder skip their own clears.
+// Enqueue compress; the result record lands in res_out (device; default
+// ws.result).  One launch clears what the passes expect zeroed (the
+// value-range pass's ticket and the result record among it), so the
+// value-range pass and the encoder skip their own clears.
 static int enqueue_compress(int mode, int dtype, const void* d_x, size_t n, int bs, int err_mode, float abs_eb,
-                            float rel, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s) {
+                            float rel, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s,
+                            StreamResult* res_out = nullptr) {
     cudaError_t e;
+    if (n == 0 || (mode != kNonBlocked && bs < 1)) return cuda_fail(cudaErrorInvalidValue);
+    ClearList c = mode == kNonBlocked ? nonblocked_enc_clear(ws, n) : blocked_enc_clear(ws, (n + bs - 1) / bs);
+    if (res_out) {
+        c.p[c.n] = res_out;
+        c.bytes[c.n] = sizeof(StreamResult);
+        c.n++;
+    }
+    if ((e = launch_ws_clear(c, s)) != cudaSuccess) return cuda_fail(e);
     if (mode == kNonBlocked) {
-        if ((e = launch_ws_clear(nonblocked_enc_clear(ws, n), s)) != cudaSuccess) return cuda_fail(e);
         if ((e = launch_range(dtype, d_x, n, err_mode, abs_eb, rel, ws, s, true)) != cudaSuccess) return cuda_fail(e);
-        if ((e = launch_nonblocked_encode(dtype, d_x, n, d_out, cap, ws, s, true)) != cudaSuccess)
+        if ((e = launch_nonblocked_encode(dtype, d_x, n, d_out, cap, ws, s, true, res_out)) != cudaSuccess)
             return cuda_fail(e);
         return SZXG_OK;
     }
     bool use_params = err_mode == REL;
-    if (n == 0 || bs < 1) return cuda_fail(cudaErrorInvalidValue);
-    if ((e = launch_ws_clear(blocked_enc_clear(ws, (n + bs - 1) / bs), s)) != cudaSuccess) return cuda_fail(e);
     if (use_params && (e = launch_range(dtype, d_x, n, err_mode, abs_eb, rel, ws, s, true)) != cudaSuccess)
         return cuda_fail(e);
-    if ((e = launch_blocked_encode(mode, dtype, d_x, n, bs, use_params, abs_eb, d_out, cap, ws, s, true)) !=
+    if ((e = launch_blocked_encode(mode, dtype, d_x, n, bs, use_params, abs_eb, d_out, cap, ws, s, true, res_out)) !=
         cudaSuccess)
         return cuda_fail(e);
     return SZXG_OK;
@@ -385,7 +392,6 @@ static void* host_decompress(int mode, int dtype, const unsigned char* bytes, si
     uint8_t* d_s = (uint8_t*)c->in.p + pad;
     cudaError_t e = cudaMemcpyAsync(d_s, bytes, len, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) { drop(); cuda_fail(e); return nullptr; }
-    if (cudaMemsetAsync(ws.err, 0, sizeof(int), s) != cudaSuccess) { drop(); set_err(SZXG_ERR_CUDA); return nullptr; }
     if (enqueue_decompress(mode, dtype, d_s, len, n, bs, c->out.p, ws, s)) { drop(); return nullptr; }
     int err = 0;
     if (own) {
@@ -742,11 +748,14 @@ int SZxG_compress(int fastMode, int dataType, const void* d_data, size_t nbEle, 
     }
     cudaStream_t s = (cudaStream_t)stream;
     Workspace ws = ws_carve(d_workspace, fastMode, dataType, nbEle, blockSize);
+    static_assert(sizeof(SZxG_StreamInfo) == sizeof(StreamResult), "info layout");
+    // the kernels write the result record straight into an 8-byte aligned
+    // d_info; any other d_info gets a copy of it
+    const bool direct = d_info && ((uintptr_t)d_info & 7) == 0;
     int rc = enqueue_compress(fastMode, dataType, d_data, nbEle, blockSize, errBoundMode, absErrBound, relBoundRatio,
-                              (uint8_t*)d_out, outCapacity, ws, s);
+                              (uint8_t*)d_out, outCapacity, ws, s, direct ? (StreamResult*)d_info : nullptr);
     if (rc) return rc;
-    if (d_info) {
-        static_assert(sizeof(SZxG_StreamInfo) == sizeof(StreamResult), "info layout");
+    if (d_info && !direct) {
         cudaError_t e = cudaMemcpyAsync(d_info, ws.result, sizeof(StreamResult), cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) return cuda_fail(e);
     }
@@ -786,7 +795,7 @@ int SZxG_decompress(int fastMode, int dataType, const void* d_stream, size_t str
     }
     if (workspaceBytes < ws_bytes(fastMode, dataType, nbEle, blockSize)) { set_err(SZXG_ERR_ARG); return SZXG_ERR_ARG; }
     Workspace ws = ws_carve(d_workspace, fastMode, dataType, nbEle, blockSize);
-    if (cudaMemsetAsync(ws.err, 0, sizeof(int), s) != cudaSuccess) return cuda_fail(cudaErrorUnknown);
+    // (the first kernel of every decode, the header parse, sets ws.err)
     int rc = enqueue_decompress(fastMode, dataType, (const uint8_t*)d_stream, streamBytes, nbEle, blockSize, d_out, ws,
                                 s);
     if (rc == SZXG_OK) set_err(SZXG_OK);

@@ -879,7 +879,7 @@ ClearList blocked_enc_clear(const Workspace& ws, size_t nb) {
 
 cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
                                   float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s,
-                                  bool cleared) {
+                                  bool cleared, StreamResult* res_out) {
     if (n == 0 || bs < 1 || bs > 256) return cudaErrorInvalidValue;
     if (layout == kBlocked && bs > 255) return cudaErrorInvalidValue;
     const size_t nb = (n + bs - 1) / bs, sb = (nb + 7) / 8;
@@ -903,7 +903,7 @@ cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n
     F.st_asm = ws.st_word + enc_status_words(nb);   // encoder's words first
     F.size_blk = ws.o_scr; F.med_blk = ws.m_scr; F.s_scr = ws.s_scr;
     F.tot = ws.totals;
-    F.res = ws.result;
+    F.res = res_out ? res_out : ws.result;
     return launch_blocked_encode_fields(layout, dtype, bs, 1, F, nullptr, nullptr, F.enc_tiles, F.asm_tiles,
                                         ws.counters, ws.err, s, LaunchShape{});
 }

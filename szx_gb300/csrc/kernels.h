@@ -213,10 +213,11 @@ cudaError_t launch_range(int dtype, const void* x, size_t n, int err_mode, float
 // Blocked encode (layouts 2, 3, 4): stats + encode + placement + header assembly.
 // d_out must hold blocked_bound() bytes; the stream lands at d_out + result.offset.
 size_t blocked_bound(int layout, int dtype, size_t n, int bs);
-// cleared: the caller has zeroed blocked_enc_clear()'s regions already.
+// cleared: the caller has zeroed blocked_enc_clear()'s regions already;
+// res_out: where the stream's result record goes (default ws.result).
 cudaError_t launch_blocked_encode(int layout, int dtype, const void* x, size_t n, int bs, bool use_params,
                                   float abs_eb, uint8_t* d_out, size_t cap, const Workspace& ws, cudaStream_t s,
-                                  bool cleared = false);
+                                  bool cleared = false, StreamResult* res_out = nullptr);
 // The regions a blocked encode of nb blocks expects zeroed: both look-backs'
 // status words, then totals / result / error / counters (counters[3], the
 // value-range pass's ticket, among them).
@@ -261,9 +262,11 @@ cudaError_t launch_blocked_decode(int layout, int dtype, const uint8_t* d_stream
 
 // Non-blocked (layout 1) encode / decode.
 size_t nonblocked_bound(int dtype, size_t n);
-// cleared: the caller has zeroed nonblocked_enc_clear()'s regions already.
+// cleared: the caller has zeroed nonblocked_enc_clear()'s regions already;
+// res_out: where the stream's result record goes (default ws.result).
 cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t* d_out, size_t cap,
-                                     const Workspace& ws, cudaStream_t s, bool cleared = false);
+                                     const Workspace& ws, cudaStream_t s, bool cleared = false,
+                                     StreamResult* res_out = nullptr);
 // The regions a non-blocked encode of n values expects zeroed: its tile
 // status words, then totals / result / error / counters.
 ClearList nonblocked_enc_clear(const Workspace& ws, size_t n);

@@ -413,7 +413,7 @@ ClearList nonblocked_enc_clear(const Workspace& ws, size_t n) {
 }
 
 cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t* d_out, size_t cap,
-                                     const Workspace& ws, cudaStream_t s, bool cleared) {
+                                     const Workspace& ws, cudaStream_t s, bool cleared, StreamResult* res_out) {
     if (n == 0 || cap < nonblocked_bound(dtype, n) - 64) return cudaErrorInvalidValue;
     const size_t ntiles = (n + kNbTile - 1) / kNbTile;
     cudaError_t e;
@@ -423,7 +423,7 @@ cudaError_t launch_nonblocked_encode(int dtype, const void* x, size_t n, uint8_t
     a.st = TileStatus32{ws.st32, ws.st_agg2, ws.st_inc2};
     a.tile_ctr = &ws.counters[0];
     a.err = ws.err;
-    a.res = ws.result;
+    a.res = res_out ? res_out : ws.result;
     static int per_sm[2][64] = {{0}};
     int dev = 0;
     cudaGetDevice(&dev);
