@@ -257,6 +257,13 @@ def timed_steps(L, codec, x, y, sv, n, rel, steps, ev_stream_sync=True):
     return t_start.elapsed_time(t_end), tc, td, kern
 
 
+def traffic_of(kernel: str, n: int):
+    """DRAM bytes per launch of `kernel` on n values from the committed ncu
+    summary (scaled by the value count), or None."""
+    tb, _ = read_traffic(kernel)
+    return round(tb * n) if tb else None
+
+
 def kernel_roofline(kern, name, alg_bytes, peak, peak_kind, traffic=None):
     """Roofline entry of one kernel: algorithmic bytes per launch / mean launch time."""
     ms, cnt = kern[name]
@@ -312,8 +319,10 @@ def run_mode1(args, L, x, rel, peak, peak_kind):
         "decompress_gbs": round(in_bytes * steps / (td / 1000) / 1e9, 2),
         "stream_bytes": size, "ratio": round(in_bytes / size, 4),
         "kernels_ms_per_step": {k: round(v[0] / steps, 4) for k, v in kern.items()},
-        "roofline_encode": kernel_roofline(kern, "nonblocked_encode", in_bytes + size, peak, peak_kind),
-        "roofline_decode": kernel_roofline(kern, "nonblocked_decode", in_bytes + size, peak, peak_kind),
+        "roofline_encode": kernel_roofline(kern, "nonblocked_encode", in_bytes + size, peak, peak_kind,
+                                           traffic_of("nonblocked_encode", n)),
+        "roofline_decode": kernel_roofline(kern, "nonblocked_decode", in_bytes + size, peak, peak_kind,
+                                           traffic_of("nonblocked_decode", n)),
         "stream_equal": equal, "decode_equal": dec_equal,
         "gpu_launches": sum(c for _, c in kern.values()),
     }
@@ -410,7 +419,10 @@ def run_ours(args, wl, rank, world, local_rank):
     if tb:
         roofline["traffic_source"] = tb_note
     other = dec if dom == enc else enc
-    roofline_other = kernel_roofline(kern, other, alg, peak, peak_kind)
+    to, to_note = read_traffic(other)
+    roofline_other = kernel_roofline(kern, other, alg, peak, peak_kind, round(to * n) if to else None)
+    if to:
+        roofline_other["traffic_source"] = to_note
 
     # parity of what was timed: the stream and the decoded field against the
     # oracle's block-parallel port of the reference codec (outside the timing)
