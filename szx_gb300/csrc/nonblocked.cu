@@ -811,12 +811,12 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
             const int c0 = R - (int)ld;
             const uint32_t c = c0 > 0 ? (uint32_t)c0 : 0u;
             const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
-            const uint32_t lo = __funnelshift_r(w0, w1, (q & 3) * 8);
+            const uint32_t lo = __funnelshift_r(w0, w1, q << 3);   // the shift wraps: (q & 3) * 8
             if constexpr (sizeof(T) == 4) {
                 sp[e] = (lo & __funnelshift_lc(0xFFFFFFFFu, 0u, 8 * c)) << (8 * (W - R));   // low c bytes (c <= 4)
             } else {
                 const uint32_t w2 = buf[(q >> 2) + 2];
-                const uint32_t hi = __funnelshift_r(w1, w2, (q & 3) * 8);
+                const uint32_t hi = __funnelshift_r(w1, w2, q << 3);
                 const unsigned long long v = ((unsigned long long)hi << 32) | lo;
                 const unsigned long long m = c >= 8 ? ~0ull : ((1ull << (8 * c)) - 1);
                 sp[e] = (v & m) << (8 * (W - R));
