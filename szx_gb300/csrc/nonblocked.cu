@@ -813,7 +813,9 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
             const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
             const uint32_t lo = __funnelshift_r(w0, w1, q << 3);   // the shift wraps: (q & 3) * 8
             if constexpr (sizeof(T) == 4) {
-                sp[e] = (lo & __funnelshift_lc(0xFFFFFFFFu, 0u, 8 * c)) << (8 * (W - R));   // low c bytes (c <= 4)
+                // the low c bytes of lo, moved to bits [32 - 8R, 32 - 8 ld): pushed to
+                // the top (a shift of 32 clears all, c = 0) and back down by the lead
+                sp[e] = __funnelshift_lc(0u, lo, 32 - 8 * c) >> (8 * ld);
             } else {
                 const uint32_t w2 = buf[(q >> 2) + 2];
                 const uint32_t hi = __funnelshift_r(w1, w2, q << 3);
