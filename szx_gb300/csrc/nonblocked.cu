@@ -812,20 +812,19 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
             const uint32_t c = c0 > 0 ? (uint32_t)c0 : 0u;
             const uint32_t w0 = buf[q >> 2], w1 = buf[(q >> 2) + 1];
             const uint32_t lo = __funnelshift_r(w0, w1, q << 3);   // the shift wraps: (q & 3) * 8
+            // the value's c bytes moved to the top of its R-byte window; the
+            // bytes that follow them (the next values') land in the top `ld`
+            // bytes, which the chain below takes from the previous value
             if constexpr (sizeof(T) == 4) {
-                // the low c bytes of lo, moved to bits [32 - 8R, 32 - 8 ld): pushed to
-                // the top (a shift of 32 clears all, c = 0) and back down by the lead
-                sp[e] = __funnelshift_lc(0u, lo, 32 - 8 * c) >> (8 * ld);
+                sp[e] = lo << (8 * (W - R));
             } else {
                 const uint32_t w2 = buf[(q >> 2) + 2];
                 const uint32_t hi = __funnelshift_r(w1, w2, q << 3);
-                const unsigned long long v = ((unsigned long long)hi << 32) | lo;
-                const unsigned long long m = c >= 8 ? ~0ull : ((1ull << (8 * c)) - 1);
-                sp[e] = (v & m) << (8 * (W - R));
+                sp[e] = (((unsigned long long)hi << 32) | lo) << (8 * (W - R));
             }
             q += c;
             const U inh = ~((~(U)0) >> (8 * ld));   // the top `ld` bytes come from the previous value
-            prev0 = sp[e] | (prev0 & inh);
+            prev0 = (sp[e] & ~inh) | (prev0 & inh);
         }
         // (top bytes, byte mask) pairs: a later pair's masked bytes win,
         // masks accumulate -- one three-input logic op each
@@ -857,7 +856,7 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
         for (int e = 0; e < kNbPer; e++) {
             const uint32_t ld = (codes >> (8 * (e >> 2) + 6 - 2 * (e & 3))) & 3;
             const U inh = ~((~(U)0) >> (8 * ld));
-            const U cur = sp[e] | (prev & inh);
+            const U cur = (sp[e] & ~inh) | (prev & inh);
             sp[e] = cur << sft;
             v[e] = EL::add(EL::of(sp[e]), med);
             bad |= v[e] != v[e];
