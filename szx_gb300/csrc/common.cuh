@@ -49,6 +49,18 @@ template <> struct Elem<double> {
 // float<->double conversions keep the payload.  CUDA returns one canonical
 // NaN instead.  These helpers restore the x86 result; the hot loops call the
 // plain operation and take the fix-up path only when a warp saw a NaN.
+// max with NaN propagation (a NaN input gives a NaN), two and three inputs
+// (the three-input form is sm_100 and later)
+__device__ __forceinline__ float fmax_nan(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float fmax3_nan(float a, float b, float c) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
 __device__ __forceinline__ float nan_rule(float a, float b) {
     uint32_t ua = __float_as_uint(a), ub = __float_as_uint(b);
     if ((ua & 0x7FFFFFFFu) > 0x7F800000u) return __uint_as_float(ua | 0x00400000u);

@@ -859,8 +859,15 @@ __global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 3 : 2)
             const U cur = (sp[e] & ~inh) | (prev & inh);
             sp[e] = cur << sft;
             v[e] = EL::add(EL::of(sp[e]), med);
-            bad |= v[e] != v[e];
+            if constexpr (sizeof(T) != 4) bad |= v[e] != v[e];
             prev = cur;
+        }
+        if constexpr (sizeof(T) == 4) {   // a NaN anywhere: three-input max with NaN propagation
+            float hn = v[0];
+#pragma unroll
+            for (int e = 1; e + 1 < kNbPer; e += 2) hn = fmax3_nan(hn, v[e], v[e + 1]);
+            hn = fmax_nan(hn, v[kNbPer - 1]);
+            bad = hn != hn;
         }
         if (__any_sync(0xffffffffu, bad)) {
 #pragma unroll

@@ -89,13 +89,8 @@ __device__ __forceinline__ void store_chunks(T* ob, int len, bool vec, const T (
     }
 }
 
-__device__ __forceinline__ float fmax_nan(float a, float b) {
-    float r;
-    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
-    return r;
-}
 // Three-input forms (sm_100 and later): NaN inputs are ignored like fminf /
-// fmaxf, or propagated like fmax_nan.
+// fmaxf (fmax_nan / fmax3_nan, which propagate them, are in common.cuh).
 __device__ __forceinline__ float fmin3(float a, float b, float c) {
     float r;
     asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
@@ -104,11 +99,6 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
     float r;
     asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-__device__ __forceinline__ float fmax3_nan(float a, float b, float c) {
-    float r;
-    asm("max.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
 }
 // bytes [0, n) of a word set (n <= 0: none, n >= 4: all)
